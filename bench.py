@@ -1,0 +1,381 @@
+#!/usr/bin/env python3
+"""Benchmark of the irregular CSR neighbour-expansion path on GB300.
+
+Headline workload (one "step"): a 20-sweep pull PageRank (damping 0.85, out-degree normalised,
+dangling mass spread uniformly) over a seeded R-MAT graph of scale 22 and edge factor 16
+(4,194,304 vertices, 67,108,864 arcs). Metric: GTEPS = arcs x sweeps / second, whole job.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl dpg|reference] [--no-extra]
+
+* value: device-resident inputs, CUDA events around K steps on the launching stream.
+* e2e: the one-shot C-ABI call with host buffers (pinned), H2D of the transposed CSR and
+  out-degrees and D2H of the ranks inside the timed region.
+* roofline: the row-gather kernel's algorithmic bytes per sweep / its average launch time from
+  CUDA events recorded around every launch inside the timed region.
+* cpu_baseline / --impl reference: the CPU restatement of the reference's PageRank (the reference
+  has no CPU PageRank), all host threads, timed on a bounded sample.
+* extra: SpMV on the same graph, SSSP and BFS on R-MAT scale 24 (268,435,456 arcs).
+Multi-GPU (torchrun): replicas only, one independent copy of the workload per rank; time = max over
+ranks; value = all ranks' arcs x sweeps / that time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GTEPS (SSSP/PageRank) on 1 GB300, % of HBM roofline; batched+adjoint vs plain"
+SCALE, EDGE_FACTOR, SWEEPS, DAMPING, GRAPH_SEED = 22, 16, 20, 0.85, 22
+WORKLOAD = (f"pagerank-pull rmat(0.57,0.19,0.19,0.05) scale {SCALE} edge-factor {EDGE_FACTOR}, "
+            f"{SWEEPS} sweeps, d={DAMPING}")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["dpg", "reference"], default="dpg")
+    ap.add_argument("--no-extra", action="store_true", help="skip the SpMV / SSSP / BFS side measurements")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name: str):
+    """DRAM bytes per launch recorded in profiles/<name> by an ncu capture (None when absent)."""
+    p = ROOT / "profiles" / name
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_full_launch"):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+def build_workload(dpg):
+    g = dpg.rmat_csr(SCALE, EDGE_FACTOR, seed=GRAPH_SEED, weights=False)
+    in_off, in_col = dpg.csr_transpose(g.V, g.offsets, g.col)
+    od = dpg.out_degrees(g.offsets)
+    return g, in_off, in_col, od
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.proc = None
+        self.lines: list[str] = []
+        cmd = ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "50"]
+        if gpu_id:
+            cmd += ["-i", gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.12)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_pagerank_sample(orc, in_off, in_col, od, E, target_s=10.0):
+    """Times the CPU restatement (all host threads) on whole 20-sweep solves, repeated to ~target_s."""
+    threads = orc.num_threads()
+    t0 = time.perf_counter()
+    orc.pagerank_omp_f32(in_off, in_col, od, damping=DAMPING, total=1.0, iterations=1)
+    one = time.perf_counter() - t0
+    sweeps = SWEEPS if one * SWEEPS <= target_s else max(1, int(target_s / max(one, 1e-9)))
+    reps = max(1, int(target_s / max(one * sweeps, 1e-9)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        orc.pagerank_omp_f32(in_off, in_col, od, damping=DAMPING, total=1.0, iterations=sweeps)
+    dt = time.perf_counter() - t0
+    return {"value": E * sweeps * reps / dt / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
+            "sample": f"{reps} x {sweeps}-sweep pull PageRank on the full scale-{SCALE} graph ({dt:.1f} s, "
+                      f"CPU restatement: the reference has no CPU PageRank)"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    import __graft_entry__
+
+    dpg = __graft_entry__.load_package()
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+
+    g, in_off, in_col, od = build_workload(dpg)
+    threads = orc.num_threads()
+    t0 = time.perf_counter()
+    orc.pagerank_omp_f32(in_off, in_col, od, damping=DAMPING, total=1.0, iterations=1)
+    one = time.perf_counter() - t0
+    sweeps = SWEEPS if one * SWEEPS <= 3.0 else max(1, int(3.0 / max(one, 1e-9)))
+    for _ in range(args.warmup):
+        orc.pagerank_omp_f32(in_off, in_col, od, damping=DAMPING, total=1.0, iterations=sweeps)
+    steps = min(args.steps, 20)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        orc.pagerank_omp_f32(in_off, in_col, od, damping=DAMPING, total=1.0, iterations=sweeps)
+    dt = time.perf_counter() - t0
+    value = g.E * sweeps * steps / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "vertices": g.V, "arcs": g.E, "sweeps_per_step": sweeps,
+                   "note": "CPU restatement of pagerank_thread_pull_kernel + host loop; all host threads"},
+        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
+                         "sample": f"{steps} steps x {sweeps} sweeps on the full graph"},
+        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def extra_measurements(dpg, ctx, torch, g, peak, steps):
+    """SpMV on the scale-22 graph; SSSP and BFS on R-MAT scale 24 (device-resident, CUDA events)."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    out = {}
+    V, E = g.V, g.E
+    rng = np.random.default_rng(22)
+    vals = torch.from_numpy((1.0 - rng.random(E, dtype=np.float32)).astype(np.float32)).to(dev)
+    x = torch.from_numpy(rng.uniform(-1, 1, V).astype(np.float32)).to(dev)
+    y = torch.empty(V, dtype=torch.float32, device=dev)
+    dg = dpg.Graph(ctx, g.offsets, g.col)
+    for _ in range(3):
+        dpg.spmv_dev(ctx, dg, vals.data_ptr(), x.data_ptr(), y.data_ptr())
+    ctx.profile_reset()
+    n = max(20, steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(n):
+        dpg.spmv_dev(ctx, dg, vals.data_ptr(), x.data_ptr(), y.data_ptr())
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / n
+    lg, msg = ctx.profile_read(dpg.KERNEL_ROWGATHER)
+    bytes_spmv = 4 * (V + 1) + 8 * E + 8 * V
+    out["spmv_rmat22"] = {"gteps": E / (t / 1e3) / 1e9, "ms": t, "gather_ms": msg / max(lg, 1),
+                          "roofline_frac": bytes_spmv / (msg / max(lg, 1) / 1e3) / 1e9 / peak,
+                          "bytes_per_launch": bytes_spmv}
+    del dg, vals, x, y
+
+    g24 = dpg.rmat_csr(24, 16, seed=24, wmin=1, wmax=255)
+    V24, E24 = g24.V, g24.E
+    dg24 = dpg.Graph(ctx, g24.offsets, g24.col, g24.weights)
+    deg = np.diff(g24.offsets)
+    srcs = [int(s) for s in np.random.default_rng(24).choice(np.flatnonzero(deg > 0), 4, replace=False)]
+    label = torch.empty(V24, dtype=torch.int32, device=dev)
+    for name, fn, bytes_pass in (("sssp_rmat24", dpg.sssp_dev, 4 * (V24 + 1) + 8 * E24 + 8 * V24),
+                                 ("bfs_rmat24", dpg.bfs_dev, 4 * (V24 + 1) + 4 * E24 + 8 * V24)):
+        fn(ctx, dg24, srcs[0], label.data_ptr())
+        ctx.synchronize()
+        times, kms, scanned, iters = [], [], [], []
+        for s in srcs:
+            ctx.profile_reset()
+            e0.record()
+            fn(ctx, dg24, s, label.data_ptr())
+            e1.record()
+            torch.cuda.synchronize()
+            ctx.synchronize()
+            times.append(e0.elapsed_time(e1))
+            _, km = ctx.profile_read(dpg.KERNEL_EXPAND)
+            kms.append(km)
+            st = ctx.last_stats()
+            scanned.append(st.edges_scanned / E24)
+            iters.append(st.iterations)
+        t = statistics.median(times)
+        km = statistics.median(kms)
+        out[name] = {"gteps": E24 / (t / 1e3) / 1e9, "ms": t, "kernel_ms": km,
+                     "roofline_frac": bytes_pass / (km / 1e3) / 1e9 / peak, "bytes_per_solve": bytes_pass,
+                     "edges_scanned_over_E": statistics.median(scanned), "iterations": statistics.median(iters),
+                     "sources": srcs}
+    return out
+
+
+def run_dpg(args, world, rank, local):
+    import torch
+
+    import __graft_entry__
+
+    dpg = __graft_entry__.load_package()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl", device_id=dev)
+    peak, peak_kind = measured_peaks()
+
+    g, in_off, in_col, od = build_workload(dpg)
+    V, E = g.V, g.E
+    ctx = dpg.Context(local)
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    gi = dpg.Graph(ctx, in_off, in_col)
+    od_t = torch.from_numpy(od).to(dev)
+    rank_t = torch.empty(V, dtype=torch.float32, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        dpg.pagerank_dev(ctx, gi, od_t.data_ptr(), rank_t.data_ptr(), damping=DAMPING, iterations=SWEEPS)
+    ctx.synchronize()
+
+    gpu_id = None
+    try:
+        gpu_id = str(torch.cuda.get_device_properties(dev).uuid)
+        gpu_id = gpu_id if gpu_id.startswith("GPU-") else f"GPU-{gpu_id}"
+    except Exception:
+        gpu_id = None
+    ctx.profile(True)
+    ctx.profile_reset()
+    sampler = ClockSampler(gpu_id) if rank == 0 else None
+    time.sleep(0.1)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        dpg.pagerank_dev(ctx, gi, od_t.data_ptr(), rank_t.data_ptr(), damping=DAMPING, iterations=SWEEPS)
+    e1.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop() if sampler else None
+    ctx.synchronize()
+    t_ms = e0.elapsed_time(e1)
+    t_max = t_ms
+    if world > 1:
+        tt = torch.tensor([t_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    n_g, ms_g = ctx.profile_read(dpg.KERNEL_ROWGATHER)
+    n_f, ms_f = ctx.profile_read(dpg.KERNEL_FIXUP)
+    n_i, ms_i = ctx.profile_read(dpg.KERNEL_INIT)
+    ctx.profile(False)
+    value = E * SWEEPS * args.steps * world / (t_max / 1e3) / 1e9
+    gather_avg_ms = ms_g / max(n_g, 1)
+    bytes_sweep = 4 * (V + 1) + 4 * E + 12 * V  # in-offsets, in-arcs, contrib read, contrib write, outdeg read
+    achieved = bytes_sweep / (gather_avg_ms / 1e3) / 1e9
+    traffic = profile_traffic("rowgather_pagerank_rmat22.md")
+
+    # e2e: one-shot C-ABI call with pinned host buffers (upload, solve, download inside the region).
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    h_off, h_col, h_od = pin(in_off), pin(in_col), pin(od)
+    h_rank = torch.empty(V, dtype=torch.float32).pin_memory().numpy()
+    dpg.pagerank_host(ctx, h_off, h_col, h_od, out=h_rank, damping=DAMPING, iterations=SWEEPS)
+    e2e_steps = max(3, min(args.steps, 10))
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        dpg.pagerank_host(ctx, h_off, h_col, h_od, out=h_rank, damping=DAMPING, iterations=SWEEPS)
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([t_e2e], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e_value = E * SWEEPS * e2e_steps * world / t_e2e / 1e9
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "vertices": V, "arcs": E, "graph_seed": GRAPH_SEED,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (in-arcs 268 MB > 129 MB), no flush"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "rowgather_kernel<PageRank>", "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": bytes_sweep, "avg_launch_ms": gather_avg_ms},
+        "e2e": {"value": e2e_value, "unit": "GTEPS", "steps": e2e_steps,
+                "h2d_bytes_per_step": int(h_off.nbytes + h_col.nbytes + h_od.nbytes),
+                "d2h_bytes_per_step": int(h_rank.nbytes)},
+        "gpu_launches": int(n_g + n_f + n_i),
+        "kernel_ms": {"rowgather": ms_g, "fixup": ms_f, "init": ms_i},
+    }
+    if clocks:
+        line["clocks"] = clocks
+    if world == 1:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as orc
+
+        line["cpu_baseline"] = cpu_pagerank_sample(orc, in_off, in_col, od, E)
+        if not args.no_extra:
+            del gi
+            line["extra"] = extra_measurements(dpg, ctx, torch, g, peak, args.steps)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main() -> int:
+    args = parse_args()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_dpg(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

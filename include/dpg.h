@@ -1,0 +1,225 @@
+/*
+ * dpg.h — C ABI of the GB300-native irregular CSR neighbour-expansion library.
+ *
+ * The reference (show-me-dynamic-parallelism) has no plugin or FFI API: each app's main() calls a
+ * zero-argument wrapper that talks through globals:
+ *     void SSSP_GPU();        apps/sssp/src/sssp.h:32
+ *     void SpMV_GPU();        apps/SpMV/src/SpMV.h:38
+ *     void PAGERANK_GPU();    apps/pagerank/src/pagerank.h:36
+ *     void BFS_REC_GPU();     apps/bfs-rec/src/bfs_rec.h:34
+ *     void GRAPH_COLOR_GPU(); apps/graph-color/src/graph_color.h:24
+ * Their inputs are the globals of common/global.h:28-58 (graph.vertexArray, graph.edgeArray,
+ * graph.weightArray, graph.childVertexArray, graph.rEdgeArray, graph.outdegreeArray, noNodeTotal,
+ * noEdgeTotal, source, config.solution, config.device_num). Their outputs are written in place into
+ * graph.costArray / y / graph.rankArray / graph.levelArray / graph.colorArray.
+ *
+ * Every entry point below replaces one of those calls (or one phase of it) with explicit pointers
+ * and sizes. The conventions are:
+ *   - every function returns dpg_status and never calls exit();
+ *   - host-pointer entry points ("e2e" calls) copy inputs to the GPU, run, and copy results back,
+ *     synchronously, like the reference wrappers;
+ *   - *_dev entry points take device pointers and are stream-ordered on the context's stream;
+ *     errors raised inside a kernel (timeout, capacity) are reported by dpg_ctx_synchronize();
+ *   - one context per host thread.
+ */
+#ifndef DPG_H
+#define DPG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DPG_VERSION 1
+
+/* Unreachable SSSP distance: INF in apps/sssp/src/sssp_wrapper.cu:5 and common/global.h:19. */
+#define DPG_INF_COST 1073741824
+/* Unreached BFS level: UNDEFINED in apps/bfs-rec/src/bfs_rec.h:13. */
+#define DPG_UNDEFINED_LEVEL 0x7FFFFFFF
+/* Degree threshold of the reference's consolidation kernels (THRESHOLD, sssp_kernel.cu:7). */
+#define DPG_REF_THRESHOLD 64
+
+typedef enum dpg_status {
+    DPG_OK = 0,
+    DPG_ERR_INVALID_ARG = 1, /* bad pointer, size, vertex id or option */
+    DPG_ERR_CAPACITY = 2,    /* a worklist or buffer would overflow, or the iteration cap was hit */
+    DPG_ERR_TIMEOUT = 3,     /* a bounded device-side wait (grid barrier) ran out */
+    DPG_ERR_CUDA = 4,        /* a CUDA runtime call failed; see dpg_last_error() */
+    DPG_ERR_NO_DEVICE = 5,   /* no usable CUDA device */
+    DPG_ERR_IO = 6,          /* file could not be opened / read / written */
+    DPG_ERR_FORMAT = 7,      /* malformed graph file */
+    DPG_ERR_UNSUPPORTED = 8  /* option combination not implemented */
+} dpg_status;
+
+/* Work-mapping strategy for the frontier expansion (the reference's -s/--solution flag).
+ * 0-4 keep the meaning of apps/sssp/src/sssp.cpp:65-70; 5 is the GB300 default. */
+typedef enum dpg_solution {
+    DPG_SOL_THREAD = 0, /* thread per frontier vertex, serial neighbour loop (unorder_threadQueue_kernel) */
+    DPG_SOL_NAIVE = 1,  /* degree >= threshold: one warp per vertex, launched per vertex (naive DP) */
+    DPG_SOL_WARP = 2,   /* degree >= threshold: consolidated per warp, expanded by the warp */
+    DPG_SOL_BLOCK = 3,  /* degree >= threshold: consolidated per CTA in shared memory, expanded by the CTA */
+    DPG_SOL_GRID = 4,   /* degree >= threshold: consolidated grid-wide, expanded by every CTA */
+    DPG_SOL_BINNED = 5  /* warp scan-gather below hub_threshold, grid-wide edge chunks above */
+} dpg_solution;
+
+typedef struct dpg_ctx dpg_ctx;
+typedef struct dpg_graph dpg_graph;
+
+typedef struct dpg_expand_opts {
+    int32_t solution;        /* dpg_solution; DPG_SOL_BINNED when the struct pointer is NULL */
+    int32_t threshold;       /* consolidation degree threshold; 0 -> DPG_REF_THRESHOLD */
+    int32_t hub_threshold;   /* BINNED: degree at which a vertex is expanded grid-wide; 0 -> auto */
+    int32_t max_iterations;  /* 0 -> V + 2 (label-correcting never needs more) */
+    double timeout_seconds;  /* limit of each grid-barrier wait; 0 -> 10 s */
+} dpg_expand_opts;
+
+typedef struct dpg_pr_opts {
+    double damping;          /* 0.85 (workload) ; 0.5 in the reference (pagerank_wrapper.cu:7) */
+    double total_rank;       /* 1.0 (workload) ; 1000 in the reference (pagerank.h:15) */
+    int32_t init_zero;       /* 1: start from rank 0 (pagerank_wrapper.cu:115); 0: total/V */
+    int32_t iterations;      /* fixed iteration count when epsilon <= 0 ; cap otherwise */
+    double epsilon;          /* > 0: iterate until every |new-old| <= epsilon (wrapper.cu:8, kernel.cu:72-81) */
+} dpg_pr_opts;
+
+typedef struct dpg_run_stats {
+    int64_t iterations;      /* frontier iterations (SSSP/BFS) or PageRank sweeps */
+    int64_t edges_scanned;   /* adjacency entries read by the expansion (>= E for label-correcting) */
+    int64_t vertices_popped; /* frontier entries processed */
+    int32_t grid_blocks;     /* CTAs of the persistent launch */
+    int32_t block_threads;
+} dpg_run_stats;
+
+/* ---- errors / version ------------------------------------------------------------------------ */
+const char* dpg_status_string(dpg_status s);
+const char* dpg_last_error(void); /* thread-local detail of the last failing call */
+int dpg_version(void);
+
+/* ---- context (replaces prepare_gpu's cudaSetDevice, e.g. sssp_wrapper.cu:54-68) --------------- */
+dpg_status dpg_ctx_create(int device, dpg_ctx** out);
+dpg_status dpg_ctx_destroy(dpg_ctx* ctx);
+/* Use an existing cudaStream_t (passed as void*) for every later call; NULL restores the own stream. */
+dpg_status dpg_ctx_set_stream(dpg_ctx* ctx, void* cuda_stream);
+/* Waits for the context's stream and returns the first device-side error raised since the last call. */
+dpg_status dpg_ctx_synchronize(dpg_ctx* ctx);
+/* Statistics of the last SSSP/BFS/PageRank call (synchronises). */
+dpg_status dpg_ctx_last_stats(dpg_ctx* ctx, dpg_run_stats* out);
+dpg_status dpg_ctx_sm_count(dpg_ctx* ctx, int32_t* out);
+
+/* ---- device graphs (replaces the cudaMalloc + H2D half of prepare_gpu, sssp_wrapper.cu:94-111) -- */
+/* Copies a host CSR (offsets[V+1], col[E], optional weights[E]) into the device layout. */
+dpg_status dpg_graph_create(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* offsets,
+                            const int32_t* col, const int32_t* weights, dpg_graph** out);
+/* Same from device pointers (copied device-to-device into the library layout). */
+dpg_status dpg_graph_create_device(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* d_offsets,
+                                   const int32_t* d_col, const int32_t* d_weights, dpg_graph** out);
+dpg_status dpg_graph_destroy(dpg_graph* g);
+dpg_status dpg_graph_info(const dpg_graph* g, int32_t* V, int64_t* E, int32_t* weighted);
+
+/* ---- SSSP (replaces SSSP_GPU, apps/sssp/src/sssp_wrapper.cu:304-341) --------------------------- */
+/* dist[v] = shortest distance from source, DPG_INF_COST when unreachable. Weights must be >= 0. */
+dpg_status dpg_sssp(dpg_ctx* ctx, const dpg_graph* g, int32_t source, const dpg_expand_opts* opts,
+                    int32_t* h_dist);
+dpg_status dpg_sssp_dev(dpg_ctx* ctx, const dpg_graph* g, int32_t source,
+                        const dpg_expand_opts* opts, int32_t* d_dist);
+
+/* ---- BFS (replaces BFS_REC_GPU, apps/bfs-rec/src/bfs_rec_wrapper.cu:240-280) ------------------- */
+/* level[v] = hop count from source, DPG_UNDEFINED_LEVEL when unreachable. */
+dpg_status dpg_bfs(dpg_ctx* ctx, const dpg_graph* g, int32_t source, const dpg_expand_opts* opts,
+                   int32_t* h_level);
+dpg_status dpg_bfs_dev(dpg_ctx* ctx, const dpg_graph* g, int32_t source,
+                       const dpg_expand_opts* opts, int32_t* d_level);
+
+/* ---- SpMV (replaces SpMV_GPU / csr_spmv_kernel, apps/SpMV/src/SpMV_kernel.cu:81-96) ------------ */
+/* y[r] = sum over row r of vals[e] * x[col[e]]; FP32 in and out, deterministic summation order. */
+dpg_status dpg_spmv_f32(dpg_ctx* ctx, const dpg_graph* g, const float* h_vals, const float* h_x,
+                        float* h_y);
+dpg_status dpg_spmv_f32_dev(dpg_ctx* ctx, const dpg_graph* g, const float* d_vals,
+                            const float* d_x, float* d_y);
+
+/* ---- PageRank pull (replaces PAGERANK_GPU / pg_pull_gpu, pagerank_wrapper.cu:199-244,366-400) -- */
+/* g_in is the transposed CSR (childVertexArray/rEdgeArray of invertGraph, global.cpp:237-277);
+ * outdeg[v] is the out-degree in the original graph (outdegreeArray, pagerank.cpp:108-113). */
+dpg_status dpg_pagerank_f32(dpg_ctx* ctx, const dpg_graph* g_in, const int32_t* h_outdeg,
+                            const dpg_pr_opts* opts, float* h_rank);
+dpg_status dpg_pagerank_f32_dev(dpg_ctx* ctx, const dpg_graph* g_in, const int32_t* d_outdeg,
+                                const dpg_pr_opts* opts, float* d_rank);
+
+/* ---- one-shot host calls: the whole reference wrapper in one call (upload, solve, download) ---- */
+dpg_status dpg_sssp_host(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* offsets,
+                         const int32_t* col, const int32_t* weights, int32_t source,
+                         const dpg_expand_opts* opts, int32_t* h_dist);
+dpg_status dpg_pagerank_f32_host(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* in_offsets,
+                                 const int32_t* in_col, const int32_t* outdeg,
+                                 const dpg_pr_opts* opts, float* h_rank);
+
+/* ---- launch accounting (no counterpart in the reference; its GPU_PROFILE counter,
+ *      sssp_kernel.cu:14-25, counts CDP launches only) ------------------------------------------- */
+typedef enum dpg_kernel_kind {
+    DPG_KERNEL_EXPAND = 0,    /* persistent SSSP/BFS frontier kernel */
+    DPG_KERNEL_ROWGATHER = 1, /* SpMV / PageRank warp-tile gather */
+    DPG_KERNEL_FIXUP = 2,     /* hub-row fix-up and dangling reduction */
+    DPG_KERNEL_INIT = 3,      /* initialisation kernels */
+    DPG_KERNEL_KINDS = 4
+} dpg_kernel_kind;
+/* Launch counts are always kept; enable != 0 also brackets every launch with a pair of CUDA events
+ * recorded on the launching stream, so per-kind device time can be read back. */
+dpg_status dpg_ctx_profile_enable(dpg_ctx* ctx, int32_t enable);
+dpg_status dpg_ctx_profile_reset(dpg_ctx* ctx);
+/* Synchronises; launches and summed event time (ms) of one kind since the last reset. */
+dpg_status dpg_ctx_profile_read(dpg_ctx* ctx, int32_t kind, int64_t* launches, double* total_ms);
+
+/* ---- failure-detection self test --------------------------------------------------------------- */
+/* Runs the persistent kernel's grid barrier with one block missing, so its bounded wait must run
+ * out after timeout_seconds; returns DPG_ERR_TIMEOUT when the device reported it and left the
+ * context usable. */
+dpg_status dpg_selftest_barrier_timeout(dpg_ctx* ctx, double timeout_seconds);
+
+/* ---- host graph I/O and construction (common/global.cpp) -------------------------------------- */
+typedef struct dpg_host_graph {
+    int32_t V;
+    int64_t E;
+    int32_t source;    /* from the DIMACS9 's' line, 0-based; 0 when absent (global.cpp:10,43-46) */
+    int32_t* offsets;  /* [V+1] vertexArray */
+    int32_t* col;      /* [E]   edgeArray   */
+    int32_t* weights;  /* [E]   weightArray */
+} dpg_host_graph;
+
+/* format: 0 DIMACS9 (.gr), 1 DIMACS10 (.graph), 2 SLNDC edge list — the -f flag of every app.
+ * Semantics of readInputDIMACS9/10/SLNDC + convertCSR (global.cpp:29-235): 1-based ids, each
+ * vertex's neighbour order reversed with respect to the file, DIMACS10/SLNDC weights drawn with
+ * srand(7); rand()%1000+1. */
+dpg_status dpg_read_graph(const char* path, int32_t format, dpg_host_graph* out);
+void dpg_host_graph_free(dpg_host_graph* g);
+/* convertCSR on an in-memory arc list in file order (global.cpp:192-235). Outputs are caller-owned. */
+dpg_status dpg_csr_from_arcs(int32_t V, int64_t E, const int32_t* src, const int32_t* dst,
+                             const int32_t* w, int32_t* offsets, int32_t* col, int32_t* weights);
+/* invertGraph (global.cpp:237-277): transposed CSR in the reference's neighbour order. */
+dpg_status dpg_csr_transpose(int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
+                             int32_t* in_offsets, int32_t* in_col);
+/* Writes a DIMACS9 .gr file: "p sp V E", optional "s", then "a u v w" lines in arc order. */
+dpg_status dpg_write_dimacs9(const char* path, int32_t V, int64_t E, const int32_t* src,
+                             const int32_t* dst, const int32_t* w, int32_t source);
+/* outputCost / outputLevel / outputRank / outputColor text formats (global.cpp:361-399). */
+dpg_status dpg_write_cost(const char* path, int32_t V, int32_t source, const int32_t* dist);
+dpg_status dpg_write_level(const char* path, int32_t V, const int32_t* level);
+dpg_status dpg_write_rank(const char* path, int32_t V, const float* rank);
+dpg_status dpg_write_color(const char* path, int32_t V, const int32_t* color);
+
+/* ---- seeded synthetic graphs (counter-based; any arc range is reproducible on its own) --------- */
+/* R-MAT: arc e in [0,E) draws `scale` quadrant choices with probabilities a,b,c,(1-a-b-c), then a
+ * weight uniform in [wmin,wmax]; permute != 0 relabels vertices by a seeded bijection of
+ * [0, 2^scale). Arcs with an endpoint >= V are redrawn (for V not a power of two). */
+dpg_status dpg_rmat_arcs(int32_t scale, int32_t V, int64_t E, uint64_t seed, double a, double b,
+                         double c, int32_t wmin, int32_t wmax, int32_t permute, int32_t* src,
+                         int32_t* dst, int32_t* w);
+/* rows x cols 4-neighbour grid, every undirected adjacency as two arcs, weights uniform in
+ * [wmin,wmax]; E = 2*(rows*(cols-1) + cols*(rows-1)). */
+dpg_status dpg_grid_arcs(int32_t rows, int32_t cols, uint64_t seed, int32_t wmin, int32_t wmax,
+                         int32_t* src, int32_t* dst, int32_t* w);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DPG_H */

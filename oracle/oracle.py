@@ -1,0 +1,250 @@
+"""CPU oracle bindings — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs import this module, and only
+as the checker or as the timed CPU baseline. The product library (libdpg.so) never calls it.
+
+Two libraries:
+  * oracle/_build/liboracle.so — our C restatement of the reference algorithms (dpg_oracle.c);
+  * oracle/_ref/libref.so      — the reference's own host code (common/global.cpp loader + CSR +
+    invertGraph, apps/bfs-rec/src/bfs_rec.cpp bfs_cpu), compiled from the reference tree by
+    oracle/Makefile when that tree is present. It does not exist where the reference is absent.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from ctypes import c_char_p, c_double, c_float, c_int, c_int32, c_int64, c_longlong, c_void_p, POINTER
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "_build" / "liboracle.so"
+REF_SO = HERE / "_ref" / "libref.so"
+REFERENCE_TREE = Path(os.environ.get("DPG_REFERENCE_TREE", "/root/reference"))
+
+INF = 1073741824
+UNDEFINED = 0x7FFFFFFF
+
+_P = c_void_p
+_ORACLE_SIGS = {
+    "oracle_num_threads": ([], c_int),
+    "oracle_sssp_dijkstra": ([c_int32, _P, _P, _P, c_int32, _P], c_int),
+    "oracle_sssp_worklist": ([c_int32, _P, _P, _P, c_int32, _P], c_int64),
+    "oracle_sssp_bf_omp": ([c_int32, _P, _P, _P, c_int32, _P, c_int32], c_int),
+    "oracle_bfs": ([c_int32, _P, _P, c_int32, _P], c_int64),
+    "oracle_bfs_omp": ([c_int32, _P, _P, c_int32, _P, c_int32], c_int),
+    "oracle_spmv_f64": ([c_int32, _P, _P, _P, _P, _P], None),
+    "oracle_spmv_f32in": ([c_int32, _P, _P, _P, _P, _P, _P, c_int32], None),
+    "oracle_spmv_omp_f32": ([c_int32, _P, _P, _P, _P, _P, c_int32], None),
+    "oracle_pagerank_f64": ([c_int32, _P, _P, _P, c_double, c_double, c_int32, c_int32, c_double, _P, c_int32],
+                            c_int64),
+    "oracle_pagerank_ref_f32": ([c_int32, _P, _P, _P, c_float, c_float, c_int32, c_int32, c_float, _P], c_int64),
+    "oracle_pagerank_omp_f32": ([c_int32, _P, _P, _P, c_float, c_float, c_int32, _P, c_int32], c_int64),
+    "oracle_color": ([c_int32, _P, _P, _P], c_int64),
+}
+_REF_SIGS = {
+    "ref_load": ([c_char_p, c_int, POINTER(c_int), POINTER(c_longlong), POINTER(c_int)], c_int),
+    "ref_get_csr": ([_P, _P, _P], None),
+    "ref_get_transpose": ([_P, _P], None),
+    "ref_bfs_cpu": ([c_int, _P], None),
+    "ref_output_cost": ([c_char_p, c_int, _P], c_int),
+    "ref_output_rank": ([c_char_p, _P], c_int),
+    "ref_output_color": ([c_char_p, _P], c_int),
+}
+
+_oracle = None
+_ref = None
+
+
+def build(with_reference: bool | None = None) -> None:
+    """Compiles liboracle.so, and libref.so when the reference tree is present."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    if with_reference is None:
+        with_reference = (REFERENCE_TREE / "common" / "global.cpp").exists()
+    if with_reference:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_TREE}"], check=True)
+
+
+def _load(path: Path, sigs):
+    lib = ctypes.CDLL(str(path))
+    for name, (args, res) in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    return lib
+
+
+def oracle_lib():
+    global _oracle
+    if _oracle is None:
+        if not ORACLE_SO.exists():
+            build(with_reference=False)
+        _oracle = _load(ORACLE_SO, _ORACLE_SIGS)
+    return _oracle
+
+
+def ref_available() -> bool:
+    return REF_SO.exists()
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        if not REF_SO.exists():
+            raise FileNotFoundError("oracle/_ref/libref.so is not built (the reference tree is absent here)")
+        _ref = _load(REF_SO, _REF_SIGS)
+    return _ref
+
+
+def _p(a):
+    return a.ctypes.data_as(c_void_p)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def num_threads() -> int:
+    return int(oracle_lib().oracle_num_threads())
+
+
+def sssp_dijkstra(off, col, w, src) -> np.ndarray:
+    off, col, w = _i32(off), _i32(col), _i32(w)
+    V = off.shape[0] - 1
+    d = np.empty(max(V, 1), np.int32)
+    rc = oracle_lib().oracle_sssp_dijkstra(V, _p(off), _p(col), _p(w), src, _p(d))
+    if rc != 0:
+        raise RuntimeError(f"oracle_sssp_dijkstra failed ({rc})")
+    return d[:V]
+
+
+def sssp_worklist(off, col, w, src) -> tuple[np.ndarray, int]:
+    off, col, w = _i32(off), _i32(col), _i32(w)
+    V = off.shape[0] - 1
+    d = np.empty(max(V, 1), np.int32)
+    passes = oracle_lib().oracle_sssp_worklist(V, _p(off), _p(col), _p(w), src, _p(d))
+    return d[:V], int(passes)
+
+
+def sssp_bf_omp(off, col, w, src, threads=0) -> np.ndarray:
+    off, col, w = _i32(off), _i32(col), _i32(w)
+    V = off.shape[0] - 1
+    d = np.empty(max(V, 1), np.int32)
+    if oracle_lib().oracle_sssp_bf_omp(V, _p(off), _p(col), _p(w), src, _p(d), threads) != 0:
+        raise RuntimeError("oracle_sssp_bf_omp failed")
+    return d[:V]
+
+
+def bfs(off, col, src) -> np.ndarray:
+    off, col = _i32(off), _i32(col)
+    V = off.shape[0] - 1
+    lv = np.empty(max(V, 1), np.int32)
+    if oracle_lib().oracle_bfs(V, _p(off), _p(col), src, _p(lv)) < 0:
+        raise RuntimeError("oracle_bfs failed")
+    return lv[:V]
+
+
+def bfs_omp(off, col, src, threads=0) -> np.ndarray:
+    off, col = _i32(off), _i32(col)
+    V = off.shape[0] - 1
+    lv = np.empty(max(V, 1), np.int32)
+    if oracle_lib().oracle_bfs_omp(V, _p(off), _p(col), src, _p(lv), threads) != 0:
+        raise RuntimeError("oracle_bfs_omp failed")
+    return lv[:V]
+
+
+def spmv_f64(off, col, data, x) -> np.ndarray:
+    off, col = _i32(off), _i32(col)
+    data = np.ascontiguousarray(data, np.float64)
+    x = np.ascontiguousarray(x, np.float64)
+    V = off.shape[0] - 1
+    y = np.empty(max(V, 1), np.float64)
+    oracle_lib().oracle_spmv_f64(V, _p(off), _p(col), _p(data), _p(x), _p(y))
+    return y[:V]
+
+
+def spmv_f32in(off, col, data, x, threads=0) -> tuple[np.ndarray, np.ndarray]:
+    """FP64 accumulation of FP32 products; returns (y, sum |a_ij x_j| per row)."""
+    off, col = _i32(off), _i32(col)
+    data = np.ascontiguousarray(data, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    V = off.shape[0] - 1
+    y = np.empty(max(V, 1), np.float64)
+    a = np.empty(max(V, 1), np.float64)
+    oracle_lib().oracle_spmv_f32in(V, _p(off), _p(col), _p(data), _p(x), _p(y), _p(a), threads)
+    return y[:V], a[:V]
+
+
+def spmv_omp_f32(off, col, data, x, threads=0) -> np.ndarray:
+    off, col = _i32(off), _i32(col)
+    data = np.ascontiguousarray(data, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    V = off.shape[0] - 1
+    y = np.empty(max(V, 1), np.float32)
+    oracle_lib().oracle_spmv_omp_f32(V, _p(off), _p(col), _p(data), _p(x), _p(y), threads)
+    return y[:V]
+
+
+def pagerank_f64(in_off, in_col, outdeg, damping=0.85, total=1.0, init_zero=False, iterations=20, epsilon=0.0,
+                 threads=0) -> tuple[np.ndarray, int]:
+    in_off, in_col, outdeg = _i32(in_off), _i32(in_col), _i32(outdeg)
+    V = in_off.shape[0] - 1
+    r = np.empty(max(V, 1), np.float64)
+    n = oracle_lib().oracle_pagerank_f64(V, _p(in_off), _p(in_col), _p(outdeg), damping, total, 1 if init_zero else 0,
+                                         iterations, epsilon, _p(r), threads)
+    return r[:V], int(n)
+
+
+def pagerank_ref_f32(in_off, in_col, outdeg, damping=0.5, total=1000.0, init_zero=True, max_iterations=10000,
+                     epsilon=1e-13) -> tuple[np.ndarray, int]:
+    in_off, in_col, outdeg = _i32(in_off), _i32(in_col), _i32(outdeg)
+    V = in_off.shape[0] - 1
+    r = np.empty(max(V, 1), np.float32)
+    n = oracle_lib().oracle_pagerank_ref_f32(V, _p(in_off), _p(in_col), _p(outdeg), damping, total,
+                                             1 if init_zero else 0, max_iterations, epsilon, _p(r))
+    return r[:V], int(n)
+
+
+def pagerank_omp_f32(in_off, in_col, outdeg, damping=0.85, total=1.0, iterations=20, threads=0) -> np.ndarray:
+    in_off, in_col, outdeg = _i32(in_off), _i32(in_col), _i32(outdeg)
+    V = in_off.shape[0] - 1
+    r = np.empty(max(V, 1), np.float32)
+    oracle_lib().oracle_pagerank_omp_f32(V, _p(in_off), _p(in_col), _p(outdeg), damping, total, iterations, _p(r),
+                                         threads)
+    return r[:V]
+
+
+def color(off, col) -> tuple[np.ndarray, int]:
+    off, col = _i32(off), _i32(col)
+    V = off.shape[0] - 1
+    c = np.empty(max(V, 1), np.int32)
+    n = oracle_lib().oracle_color(V, _p(off), _p(col), _p(c))
+    return c[:V], int(n)
+
+
+# ----------------------------------------------------------------- the reference's own host code --
+def ref_load(path, fmt=0):
+    """The reference loader itself: returns (V, E, source, off, col, w, in_off, in_col)."""
+    lib = ref_lib()
+    V, E, s = c_int(), c_longlong(), c_int()
+    rc = lib.ref_load(str(path).encode(), fmt, ctypes.byref(V), ctypes.byref(E), ctypes.byref(s))
+    if rc != 0:
+        raise RuntimeError(f"ref_load failed ({rc})")
+    n, m = V.value, E.value
+    off = np.empty(n + 1, np.int32)
+    col = np.empty(max(m, 1), np.int32)
+    w = np.empty(max(m, 1), np.int32)
+    lib.ref_get_csr(_p(off), _p(col), _p(w))
+    in_off = np.empty(n + 1, np.int32)
+    in_col = np.empty(max(m, 1), np.int32)
+    lib.ref_get_transpose(_p(in_off), _p(in_col))
+    return n, m, s.value, off, col[:m], w[:m], in_off, in_col[:m]
+
+
+def ref_bfs_cpu(src, V) -> np.ndarray:
+    """bfs_cpu of the reference on the graph loaded last by ref_load."""
+    lv = np.empty(max(V, 1), np.int32)
+    ref_lib().ref_bfs_cpu(src, _p(lv))
+    return lv[:V]

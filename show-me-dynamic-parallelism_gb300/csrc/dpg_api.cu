@@ -1,0 +1,772 @@
+// C ABI of the dpg library: contexts, device graphs, and the solver entry points that replace the
+// reference wrappers SSSP_GPU / BFS_REC_GPU / SpMV_GPU / PAGERANK_GPU (see include/dpg.h).
+//
+// Ownership: a dpg_ctx owns a device status block and a grow-only arena of scratch buffers, so
+// repeated solves on graphs of the same size allocate nothing. A dpg_graph owns its device CSR and
+// a host copy of the offsets used to plan row tiles.
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dpg_internal.h"
+#include "dpg_kernels.h"
+
+namespace dpg {
+
+thread_local std::string g_last_error;
+
+dpg_status set_error(dpg_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+
+}  // namespace dpg
+
+using namespace dpg;
+
+#define DPG_CUDA_TRY(call)                                                                       \
+    do {                                                                                         \
+        cudaError_t _e = (call);                                                                 \
+        if (_e != cudaSuccess)                                                                   \
+            return set_error(DPG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+#define DPG_TRY(expr)                  \
+    do {                               \
+        dpg_status _s = (expr);        \
+        if (_s != DPG_OK) return _s;   \
+    } while (0)
+
+namespace dpg_api {
+
+enum Slot {
+    S_QV0, S_QV1, S_QSE0, S_QSE1, S_BMP0, S_BMP1, S_HV0, S_HV1, S_HSE0, S_HSE1, S_HCP0, S_HCP1,
+    S_HOW0, S_HOW1, S_QCOUNT, S_HCOUNT, S_LABEL, S_CONTRIB0, S_CONTRIB1, S_RANK0, S_RANK1,
+    S_PARTIAL, S_DPART, S_DFIX, S_DSUM, S_NONSTOP, S_VALS, S_X, S_Y, S_OUTDEG, S_RANKOUT,
+    S_COUNT_SLOTS
+};
+
+struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+// Counts every kernel launch by kind; when enabled, brackets each launch with a CUDA event pair on
+// the launching stream so the device time of each kind can be summed afterwards.
+struct Profiler : LaunchHook {
+    bool enabled = false;
+    int64_t launches[DPG_KERNEL_KINDS] = {};
+    double ms[DPG_KERNEL_KINDS] = {};
+    struct Pending {
+        cudaEvent_t a, b;
+        int kind;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t open = nullptr;
+
+    cudaEvent_t take() {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+    void begin(int kind, cudaStream_t s) override {
+        if (kind >= 0 && kind < DPG_KERNEL_KINDS) ++launches[kind];
+        if (!enabled) return;
+        open = take();
+        cudaEventRecord(open, s);
+    }
+    void end(int kind, cudaStream_t s) override {
+        if (!enabled || !open) return;
+        cudaEvent_t b = take();
+        cudaEventRecord(b, s);
+        pending.push_back({open, b, kind});
+        open = nullptr;
+        if (pending.size() > 65536) drain();
+    }
+    // Accumulates finished pairs; synchronises on their end events.
+    void drain() {
+        for (auto& p : pending) {
+            float t = 0.f;
+            cudaEventSynchronize(p.b);
+            if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess && p.kind >= 0 && p.kind < DPG_KERNEL_KINDS)
+                ms[p.kind] += t;
+            pool.push_back(p.a);
+            pool.push_back(p.b);
+        }
+        pending.clear();
+    }
+    void reset() {
+        drain();
+        for (auto& x : launches) x = 0;
+        for (auto& x : ms) x = 0.0;
+    }
+    ~Profiler() override {
+        for (auto& p : pending) {
+            cudaEventDestroy(p.a);
+            cudaEventDestroy(p.b);
+        }
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+
+}  // namespace dpg_api
+
+using namespace dpg_api;
+
+struct dpg_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    DevStatus* st = nullptr;
+    Buf bufs[S_COUNT_SLOTS];
+    int last_grid = 0;
+    int last_block = 0;
+    int64_t last_host_iterations = -1;  // PageRank sweeps (host-counted); -1: read from the device
+    Profiler prof;
+};
+
+struct dpg_graph {
+    dpg_ctx* ctx = nullptr;
+    int32_t V = 0;
+    int64_t E = 0;
+    bool weighted = false;
+    int32_t* off = nullptr;
+    int32_t* col = nullptr;
+    int2* adj = nullptr;
+    std::vector<int32_t> h_off;
+    int32_t max_degree = 0;
+    bool plan_ready = false;
+    RowPlanDev plan;
+};
+
+namespace dpg_api {
+
+dpg_status use_device(dpg_ctx* c) {
+    if (!c) return set_error(DPG_ERR_INVALID_ARG, "null context");
+    DPG_CUDA_TRY(cudaSetDevice(c->device));
+    return DPG_OK;
+}
+
+void* arena(dpg_ctx* c, Slot s, size_t bytes, dpg_status* status) {
+    Buf& b = c->bufs[s];
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return b.p;
+    if (b.p) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        *status = set_error(DPG_ERR_CAPACITY, std::string("device allocation failed: ") + cudaGetErrorString(e));
+        return nullptr;
+    }
+    b.bytes = bytes;
+    return b.p;
+}
+
+// Reads and clears the device-side error word after the stream drains.
+dpg_status check_device(dpg_ctx* c) {
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    int err[2] = {0, 0};
+    DPG_CUDA_TRY(cudaMemcpy(err, c->st, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err[0] != 0) {
+        DPG_CUDA_TRY(cudaMemset(c->st, 0, sizeof(int) * 2));
+        const dpg_status s = static_cast<dpg_status>(err[0]);
+        return set_error(s, std::string("device reported ") + dpg_status_string(s) + " (site " + std::to_string(err[1]) + ")");
+    }
+    return DPG_OK;
+}
+
+__global__ void validate_interleave_kernel(const int32_t* col, const int32_t* w, int2* adj, int64_t E, int32_t V,
+                                           int* bad) {
+    for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < E;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int32_t c = col[e];
+        if (c < 0 || c >= V) atomicOr(bad, 1);
+        if (w) {
+            const int32_t wt = w[e];
+            if (wt < 0 || wt >= DPG_INF_COST) atomicOr(bad, 2);
+            if (adj) adj[e] = make_int2(c, wt);
+        }
+    }
+}
+
+dpg_status validate_offsets(const int32_t* off, int32_t V, int64_t E, int32_t* max_deg) {
+    if (off[0] != 0 || static_cast<int64_t>(off[V]) != E)
+        return set_error(DPG_ERR_INVALID_ARG, "offsets must start at 0 and end at E");
+    int32_t md = 0;
+    for (int32_t v = 0; v < V; ++v) {
+        const int32_t d = off[v + 1] - off[v];
+        if (d < 0) return set_error(DPG_ERR_INVALID_ARG, "offsets decrease at vertex " + std::to_string(v));
+        if (d > md) md = d;
+    }
+    *max_deg = md;
+    return DPG_OK;
+}
+
+dpg_status graph_finish(dpg_ctx* c, dpg_graph* g, const int32_t* d_w_src) {
+    // Range-check columns (and weights), and interleave (neighbour, weight) pairs for SSSP.
+    dpg_status st = DPG_OK;
+    int* bad = static_cast<int*>(arena(c, S_NONSTOP, sizeof(int) * 4, &st));
+    if (!bad) return st;
+    DPG_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), c->stream));
+    if (g->E > 0) {
+        const int blocks = c->sm_count * 4;
+        validate_interleave_kernel<<<blocks, 256, 0, c->stream>>>(g->col, d_w_src, g->adj, g->E, g->V, bad);
+        DPG_CUDA_TRY(cudaGetLastError());
+    }
+    int hbad = 0;
+    DPG_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (hbad & 1) return set_error(DPG_ERR_INVALID_ARG, "column index out of range");
+    if (hbad & 2) return set_error(DPG_ERR_INVALID_ARG, "weights must be in [0, 2^30)");
+    return DPG_OK;
+}
+
+void graph_free_device(dpg_graph* g) {
+    cudaFree(g->off);
+    cudaFree(g->col);
+    cudaFree(g->adj);
+    cudaFree(g->plan.tiles);
+    cudaFree(g->plan.hubs_small);
+    cudaFree(g->plan.hubs_big);
+    g->off = nullptr;
+    g->col = nullptr;
+    g->adj = nullptr;
+    g->plan = RowPlanDev();
+}
+
+dpg_status ensure_plan(dpg_graph* g) {
+    if (g->plan_ready) return DPG_OK;
+    RowPlanHost hp;
+    build_row_plan(g->h_off.data(), g->V, &hp);
+    RowPlanDev d;
+    d.ntiles = static_cast<int32_t>(hp.tiles.size());
+    d.nhub_small = static_cast<int32_t>(hp.hubs_small.size());
+    d.nhub_big = static_cast<int32_t>(hp.hubs_big.size());
+    d.nseg = hp.nseg;
+    cudaStream_t s = g->ctx->stream;
+    DPG_CUDA_TRY(cudaMalloc(&d.tiles, sizeof(int4) * (hp.tiles.size() + 1)));
+    DPG_CUDA_TRY(cudaMalloc(&d.hubs_small, sizeof(int4) * (hp.hubs_small.size() + 1)));
+    DPG_CUDA_TRY(cudaMalloc(&d.hubs_big, sizeof(int4) * (hp.hubs_big.size() + 1)));
+    if (!hp.tiles.empty())
+        DPG_CUDA_TRY(cudaMemcpyAsync(d.tiles, hp.tiles.data(), sizeof(int4) * hp.tiles.size(), cudaMemcpyHostToDevice, s));
+    if (!hp.hubs_small.empty())
+        DPG_CUDA_TRY(cudaMemcpyAsync(d.hubs_small, hp.hubs_small.data(), sizeof(int4) * hp.hubs_small.size(),
+                                     cudaMemcpyHostToDevice, s));
+    if (!hp.hubs_big.empty())
+        DPG_CUDA_TRY(cudaMemcpyAsync(d.hubs_big, hp.hubs_big.data(), sizeof(int4) * hp.hubs_big.size(),
+                                     cudaMemcpyHostToDevice, s));
+    DPG_CUDA_TRY(cudaStreamSynchronize(s));
+    g->plan = d;
+    g->plan_ready = true;
+    return DPG_OK;
+}
+
+void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const dpg_graph* g) {
+    if (in) *o = *in;
+    else {
+        memset(o, 0, sizeof(*o));
+        o->solution = DPG_SOL_BINNED;
+    }
+    if (o->threshold <= 0) o->threshold = DPG_REF_THRESHOLD;
+    if (o->hub_threshold <= 0) o->hub_threshold = 1024;
+    if (o->solution == DPG_SOL_GRID) o->hub_threshold = o->threshold;
+    if (o->max_iterations <= 0) {
+        const int64_t cap = static_cast<int64_t>(g->V) + 2;
+        o->max_iterations = cap > INT32_MAX ? INT32_MAX : static_cast<int32_t>(cap);
+    }
+    if (!(o->timeout_seconds > 0)) o->timeout_seconds = 10.0;
+}
+
+dpg_status run_expand(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_expand_opts* in_opts,
+                      int32_t* d_label, bool bfs) {
+    if (!g || g->ctx != c) return set_error(DPG_ERR_INVALID_ARG, "graph does not belong to this context");
+    if (!d_label && g->V > 0) return set_error(DPG_ERR_INVALID_ARG, "null output");
+    if (source < 0 || source >= g->V) return set_error(DPG_ERR_INVALID_ARG, "source vertex out of range");
+    if (!bfs && !g->weighted) return set_error(DPG_ERR_INVALID_ARG, "SSSP needs a weighted graph");
+    dpg_expand_opts o;
+    fill_expand_defaults(in_opts, &o, g);
+    if (o.solution < DPG_SOL_THREAD || o.solution > DPG_SOL_BINNED)
+        return set_error(DPG_ERR_INVALID_ARG, "unknown solution id");
+    const int32_t min_hub = (o.solution == DPG_SOL_GRID) ? o.threshold : o.hub_threshold;
+    ExpandWorkspace ws;
+    memset(&ws, 0, sizeof(ws));
+    ws.cap_v = static_cast<int64_t>(g->V) + 1;
+    expand_workspace_caps(g->V, g->E, min_hub, &ws.cap_hub, &ws.cap_chunks);
+    ws.bmp_words = (g->V + 31) / 32 + 1;
+    dpg_status st = DPG_OK;
+    const size_t nv = static_cast<size_t>(ws.cap_v);
+    ws.qv[0] = static_cast<int32_t*>(arena(c, S_QV0, nv * 4, &st));
+    ws.qv[1] = static_cast<int32_t*>(arena(c, S_QV1, nv * 4, &st));
+    ws.qse[0] = static_cast<int2*>(arena(c, S_QSE0, nv * 8, &st));
+    ws.qse[1] = static_cast<int2*>(arena(c, S_QSE1, nv * 8, &st));
+    ws.bmp[0] = static_cast<uint32_t*>(arena(c, S_BMP0, static_cast<size_t>(ws.bmp_words) * 4, &st));
+    ws.bmp[1] = static_cast<uint32_t*>(arena(c, S_BMP1, static_cast<size_t>(ws.bmp_words) * 4, &st));
+    const size_t nh = static_cast<size_t>(ws.cap_hub), nc = static_cast<size_t>(ws.cap_chunks);
+    ws.hv[0] = static_cast<int32_t*>(arena(c, S_HV0, nh * 4, &st));
+    ws.hv[1] = static_cast<int32_t*>(arena(c, S_HV1, nh * 4, &st));
+    ws.hse[0] = static_cast<int2*>(arena(c, S_HSE0, nh * 8, &st));
+    ws.hse[1] = static_cast<int2*>(arena(c, S_HSE1, nh * 8, &st));
+    ws.hcpos[0] = static_cast<int32_t*>(arena(c, S_HCP0, nh * 4, &st));
+    ws.hcpos[1] = static_cast<int32_t*>(arena(c, S_HCP1, nh * 4, &st));
+    ws.howner[0] = static_cast<int32_t*>(arena(c, S_HOW0, nc * 4, &st));
+    ws.howner[1] = static_cast<int32_t*>(arena(c, S_HOW1, nc * 4, &st));
+    ws.qcount = static_cast<uint32_t*>(arena(c, S_QCOUNT, 4 * 4, &st));
+    ws.hcount = static_cast<unsigned long long*>(arena(c, S_HCOUNT, 4 * 8, &st));
+    if (st != DPG_OK) return st;
+    ExpandLaunch L;
+    L.off = g->off;
+    L.col = g->col;
+    L.adj = g->adj;
+    L.V = g->V;
+    L.E = g->E;
+    L.label = d_label;
+    L.source = source;
+    L.bfs = bfs;
+    L.solution = o.solution;
+    L.threshold = o.threshold;
+    L.hub_threshold = o.hub_threshold;
+    L.max_iter = o.max_iterations;
+    L.timeout_ns = static_cast<unsigned long long>(o.timeout_seconds * 1e9);
+    c->last_host_iterations = -1;
+    DPG_CUDA_TRY(launch_expand(L, ws, c->st, c->stream, c->sm_count, &c->last_grid, &c->last_block, &c->prof));
+    return DPG_OK;
+}
+
+dpg_status pr_defaults(const dpg_pr_opts* in, dpg_pr_opts* o) {
+    if (in) *o = *in;
+    else {
+        o->damping = 0.85;
+        o->total_rank = 1.0;
+        o->init_zero = 0;
+        o->iterations = 20;
+        o->epsilon = 0.0;
+    }
+    if (!(o->damping >= 0.0 && o->damping <= 1.0)) return set_error(DPG_ERR_INVALID_ARG, "damping must be in [0,1]");
+    if (o->iterations < 0) return set_error(DPG_ERR_INVALID_ARG, "iterations must be >= 0");
+    if (o->epsilon > 0 && o->iterations == 0) o->iterations = INT32_MAX;
+    return DPG_OK;
+}
+
+dpg_status run_pagerank(dpg_ctx* c, dpg_graph* g, const int32_t* d_outdeg, const dpg_pr_opts* in_opts, float* d_rank) {
+    if (!g || g->ctx != c) return set_error(DPG_ERR_INVALID_ARG, "graph does not belong to this context");
+    if (g->V > 0 && (!d_outdeg || !d_rank)) return set_error(DPG_ERR_INVALID_ARG, "null outdeg or rank");
+    dpg_pr_opts o;
+    DPG_TRY(pr_defaults(in_opts, &o));
+    if (g->V == 0) return DPG_OK;
+    DPG_TRY(ensure_plan(g));
+    int gb, fb, bt;
+    rowgather_grid(c->sm_count, &gb, &fb, &bt);
+    dpg_status st = DPG_OK;
+    const size_t nv = static_cast<size_t>(g->V);
+    float* contrib[2] = {static_cast<float*>(arena(c, S_CONTRIB0, nv * 4, &st)),
+                         static_cast<float*>(arena(c, S_CONTRIB1, nv * 4, &st))};
+    float* partial = static_cast<float*>(arena(c, S_PARTIAL, static_cast<size_t>(g->plan.nseg + 1) * 4, &st));
+    double* dpart = static_cast<double*>(arena(c, S_DPART, static_cast<size_t>(gb) * (bt / 32) * 8, &st));
+    double* dfix = static_cast<double*>(arena(c, S_DFIX, static_cast<size_t>(fb) * (256 / 32) * 8, &st));
+    double* dsum = static_cast<double*>(arena(c, S_DSUM, 2 * 8, &st));
+    unsigned* nonstop = static_cast<unsigned*>(arena(c, S_NONSTOP, 16, &st));
+    const bool conv = o.epsilon > 0;
+    float* rk[2] = {nullptr, nullptr};
+    if (conv) {
+        rk[0] = static_cast<float*>(arena(c, S_RANK0, nv * 4, &st));
+        rk[1] = static_cast<float*>(arena(c, S_RANK1, nv * 4, &st));
+    }
+    if (st != DPG_OK) return st;
+    RowGatherLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.plan = g->plan;
+    L.off = g->off;
+    L.col = g->col;
+    L.vals = nullptr;
+    L.partial = partial;
+    L.V = g->V;
+    L.outdeg = d_outdeg;
+    L.damping = static_cast<float>(o.damping);
+    L.base_const = (1.0 - o.damping) * o.total_rank / static_cast<double>(g->V);
+    L.dangling_scale = o.damping / static_cast<double>(g->V);
+    L.dpart = dpart;
+    L.dfix = dfix;
+    L.epsilon = static_cast<float>(o.epsilon);
+    const float init_rank = o.init_zero ? 0.0f : static_cast<float>(o.total_rank / static_cast<double>(g->V));
+    // Initial vector: contributions into contrib[0], dangling mass into dsum[0].
+    L.y = contrib[0];
+    L.dsum_in = dsum + 1;
+    L.dsum_out = dsum;
+    float* init_rank_dst = conv ? rk[0] : (o.iterations == 0 ? d_rank : nullptr);
+    DPG_CUDA_TRY(launch_pagerank_init(L, init_rank, init_rank_dst, c->st, c->stream, c->sm_count, &c->prof));
+    int64_t sweeps = 0;
+    for (int32_t it = 0; it < o.iterations; ++it) {
+        L.x = contrib[it & 1];
+        L.y = contrib[(it + 1) & 1];
+        L.dsum_in = dsum + (it & 1);
+        L.dsum_out = dsum + ((it + 1) & 1);
+        if (conv) {
+            L.rank_prev = rk[it & 1];
+            L.rank_out = rk[(it + 1) & 1];
+            L.nonstop = nonstop;
+            DPG_CUDA_TRY(cudaMemsetAsync(nonstop, 0, sizeof(unsigned), c->stream));
+        } else {
+            L.rank_prev = nullptr;
+            L.nonstop = nullptr;
+            L.rank_out = (it == o.iterations - 1) ? d_rank : nullptr;
+        }
+        DPG_CUDA_TRY(launch_pagerank_sweep(L, c->st, c->stream, c->sm_count, &c->prof));
+        ++sweeps;
+        if (conv) {
+            unsigned h = 0;
+            DPG_CUDA_TRY(cudaMemcpyAsync(&h, nonstop, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+            DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+            if (h == 0) break;
+        }
+    }
+    if (conv) {
+        float* fin = rk[sweeps & 1];
+        DPG_CUDA_TRY(cudaMemcpyAsync(d_rank, fin, nv * 4, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    c->last_host_iterations = sweeps;
+    c->last_grid = gb;
+    c->last_block = bt;
+    return DPG_OK;
+}
+
+dpg_status run_spmv(dpg_ctx* c, dpg_graph* g, const float* d_vals, const float* d_x, float* d_y) {
+    if (!g || g->ctx != c) return set_error(DPG_ERR_INVALID_ARG, "graph does not belong to this context");
+    if (g->V == 0) return DPG_OK;
+    if (!d_x || !d_y || (g->E > 0 && !d_vals)) return set_error(DPG_ERR_INVALID_ARG, "null vals/x/y");
+    DPG_TRY(ensure_plan(g));
+    dpg_status st = DPG_OK;
+    float* partial = static_cast<float*>(arena(c, S_PARTIAL, static_cast<size_t>(g->plan.nseg + 1) * 4, &st));
+    if (st != DPG_OK) return st;
+    RowGatherLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.plan = g->plan;
+    L.off = g->off;
+    L.col = g->col;
+    L.vals = d_vals;
+    L.x = d_x;
+    L.y = d_y;
+    L.partial = partial;
+    L.V = g->V;
+    c->last_host_iterations = 1;
+    DPG_CUDA_TRY(launch_spmv(L, c->st, c->stream, c->sm_count, &c->prof));
+    return DPG_OK;
+}
+
+dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
+                               const int32_t* weights, bool device_ptrs, dpg_graph** out) {
+    if (!out) return set_error(DPG_ERR_INVALID_ARG, "null output handle");
+    *out = nullptr;
+    DPG_TRY(use_device(c));
+    if (V < 0 || E < 0 || E > INT32_MAX) return set_error(DPG_ERR_INVALID_ARG, "V must be >= 0 and 0 <= E < 2^31");
+    if (!offsets || (E > 0 && !col)) return set_error(DPG_ERR_INVALID_ARG, "null offsets or columns");
+    dpg_graph* g = new dpg_graph();
+    g->ctx = c;
+    g->V = V;
+    g->E = E;
+    g->weighted = weights != nullptr;
+    g->h_off.resize(static_cast<size_t>(V) + 1);
+    auto fail = [&](dpg_status s) {
+        graph_free_device(g);
+        delete g;
+        return s;
+    };
+    cudaError_t e;
+    if (device_ptrs) {
+        e = cudaMemcpy(g->h_off.data(), offsets, sizeof(int32_t) * (static_cast<size_t>(V) + 1), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(set_error(DPG_ERR_CUDA, std::string("offsets D2H: ") + cudaGetErrorString(e)));
+    } else {
+        memcpy(g->h_off.data(), offsets, sizeof(int32_t) * (static_cast<size_t>(V) + 1));
+    }
+    dpg_status s = validate_offsets(g->h_off.data(), V, E, &g->max_degree);
+    if (s != DPG_OK) return fail(s);
+    const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if ((e = cudaMalloc(&g->off, sizeof(int32_t) * (static_cast<size_t>(V) + 1))) != cudaSuccess ||
+        (e = cudaMalloc(&g->col, sizeof(int32_t) * static_cast<size_t>(E > 0 ? E : 1))) != cudaSuccess ||
+        (g->weighted && (e = cudaMalloc(&g->adj, sizeof(int2) * static_cast<size_t>(E > 0 ? E : 1))) != cudaSuccess))
+        return fail(set_error(DPG_ERR_CAPACITY, std::string("graph allocation: ") + cudaGetErrorString(e)));
+    if ((e = cudaMemcpyAsync(g->off, offsets, sizeof(int32_t) * (static_cast<size_t>(V) + 1), kind, c->stream)) != cudaSuccess ||
+        (E > 0 && (e = cudaMemcpyAsync(g->col, col, sizeof(int32_t) * static_cast<size_t>(E), kind, c->stream)) != cudaSuccess))
+        return fail(set_error(DPG_ERR_CUDA, std::string("graph copy: ") + cudaGetErrorString(e)));
+    const int32_t* d_w = nullptr;
+    if (g->weighted) {
+        if (device_ptrs) {
+            d_w = weights;
+        } else {
+            dpg_status as = DPG_OK;
+            int32_t* tmp = static_cast<int32_t*>(arena(c, S_VALS, sizeof(int32_t) * static_cast<size_t>(E > 0 ? E : 1), &as));
+            if (!tmp) return fail(as);
+            if (E > 0 && (e = cudaMemcpyAsync(tmp, weights, sizeof(int32_t) * static_cast<size_t>(E), cudaMemcpyHostToDevice,
+                                              c->stream)) != cudaSuccess)
+                return fail(set_error(DPG_ERR_CUDA, std::string("weights copy: ") + cudaGetErrorString(e)));
+            d_w = tmp;
+        }
+    }
+    s = graph_finish(c, g, d_w);
+    if (s != DPG_OK) return fail(s);
+    *out = g;
+    return DPG_OK;
+}
+
+}  // namespace dpg_api
+
+extern "C" {
+
+const char* dpg_status_string(dpg_status s) {
+    switch (s) {
+        case DPG_OK: return "DPG_OK";
+        case DPG_ERR_INVALID_ARG: return "DPG_ERR_INVALID_ARG";
+        case DPG_ERR_CAPACITY: return "DPG_ERR_CAPACITY";
+        case DPG_ERR_TIMEOUT: return "DPG_ERR_TIMEOUT";
+        case DPG_ERR_CUDA: return "DPG_ERR_CUDA";
+        case DPG_ERR_NO_DEVICE: return "DPG_ERR_NO_DEVICE";
+        case DPG_ERR_IO: return "DPG_ERR_IO";
+        case DPG_ERR_FORMAT: return "DPG_ERR_FORMAT";
+        case DPG_ERR_UNSUPPORTED: return "DPG_ERR_UNSUPPORTED";
+    }
+    return "DPG_ERR_UNKNOWN";
+}
+
+const char* dpg_last_error(void) { return g_last_error.c_str(); }
+
+int dpg_version(void) { return DPG_VERSION; }
+
+dpg_status dpg_ctx_create(int device, dpg_ctx** out) {
+    if (!out) return set_error(DPG_ERR_INVALID_ARG, "null output handle");
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return set_error(DPG_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= n) return set_error(DPG_ERR_INVALID_ARG, "device index out of range");
+    DPG_CUDA_TRY(cudaSetDevice(device));
+    dpg_ctx* c = new dpg_ctx();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaMalloc(&c->st, sizeof(DevStatus));
+    if (e == cudaSuccess) e = cudaMemset(c->st, 0, sizeof(DevStatus));
+    if (e != cudaSuccess) {
+        if (c->own_stream) cudaStreamDestroy(c->own_stream);
+        cudaFree(c->st);
+        delete c;
+        return set_error(DPG_ERR_CUDA, std::string("context setup: ") + cudaGetErrorString(e));
+    }
+    c->stream = c->own_stream;
+    *out = c;
+    return DPG_OK;
+}
+
+dpg_status dpg_ctx_destroy(dpg_ctx* c) {
+    if (!c) return DPG_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto& b : c->bufs) cudaFree(b.p);
+    cudaFree(c->st);
+    cudaStreamDestroy(c->own_stream);
+    delete c;
+    return DPG_OK;
+}
+
+dpg_status dpg_ctx_set_stream(dpg_ctx* c, void* stream) {
+    DPG_TRY(use_device(c));
+    c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+    return DPG_OK;
+}
+
+dpg_status dpg_ctx_synchronize(dpg_ctx* c) {
+    DPG_TRY(use_device(c));
+    return check_device(c);
+}
+
+dpg_status dpg_ctx_last_stats(dpg_ctx* c, dpg_run_stats* out) {
+    DPG_TRY(use_device(c));
+    if (!out) return set_error(DPG_ERR_INVALID_ARG, "null output");
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    DevStatus h;
+    DPG_CUDA_TRY(cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    out->iterations = c->last_host_iterations >= 0 ? c->last_host_iterations : static_cast<int64_t>(h.iterations);
+    out->edges_scanned = static_cast<int64_t>(h.edges);
+    out->vertices_popped = static_cast<int64_t>(h.pops);
+    out->grid_blocks = c->last_grid;
+    out->block_threads = c->last_block;
+    return DPG_OK;
+}
+
+dpg_status dpg_ctx_profile_enable(dpg_ctx* c, int32_t enable) {
+    DPG_TRY(use_device(c));
+    c->prof.enabled = enable != 0;
+    return DPG_OK;
+}
+
+dpg_status dpg_ctx_profile_reset(dpg_ctx* c) {
+    DPG_TRY(use_device(c));
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->prof.reset();
+    return DPG_OK;
+}
+
+dpg_status dpg_ctx_profile_read(dpg_ctx* c, int32_t kind, int64_t* launches, double* total_ms) {
+    DPG_TRY(use_device(c));
+    if (kind < 0 || kind >= DPG_KERNEL_KINDS) return set_error(DPG_ERR_INVALID_ARG, "unknown kernel kind");
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->prof.drain();
+    if (launches) *launches = c->prof.launches[kind];
+    if (total_ms) *total_ms = c->prof.ms[kind];
+    return DPG_OK;
+}
+
+dpg_status dpg_ctx_sm_count(dpg_ctx* c, int32_t* out) {
+    if (!c || !out) return set_error(DPG_ERR_INVALID_ARG, "null argument");
+    *out = c->sm_count;
+    return DPG_OK;
+}
+
+dpg_status dpg_graph_create(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
+                            const int32_t* weights, dpg_graph** out) {
+    return graph_create_common(c, V, E, offsets, col, weights, false, out);
+}
+
+dpg_status dpg_graph_create_device(dpg_ctx* c, int32_t V, int64_t E, const int32_t* d_offsets, const int32_t* d_col,
+                                   const int32_t* d_weights, dpg_graph** out) {
+    return graph_create_common(c, V, E, d_offsets, d_col, d_weights, true, out);
+}
+
+dpg_status dpg_graph_destroy(dpg_graph* g) {
+    if (!g) return DPG_OK;
+    cudaSetDevice(g->ctx->device);
+    cudaStreamSynchronize(g->ctx->stream);
+    graph_free_device(g);
+    delete g;
+    return DPG_OK;
+}
+
+dpg_status dpg_graph_info(const dpg_graph* g, int32_t* V, int64_t* E, int32_t* weighted) {
+    if (!g) return set_error(DPG_ERR_INVALID_ARG, "null graph");
+    if (V) *V = g->V;
+    if (E) *E = g->E;
+    if (weighted) *weighted = g->weighted ? 1 : 0;
+    return DPG_OK;
+}
+
+dpg_status dpg_sssp_dev(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_expand_opts* opts, int32_t* d_dist) {
+    DPG_TRY(use_device(c));
+    return run_expand(c, g, source, opts, d_dist, false);
+}
+
+dpg_status dpg_bfs_dev(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_expand_opts* opts, int32_t* d_level) {
+    DPG_TRY(use_device(c));
+    return run_expand(c, g, source, opts, d_level, true);
+}
+
+static dpg_status expand_host(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_expand_opts* opts,
+                              int32_t* h_out, bool bfs) {
+    DPG_TRY(use_device(c));
+    if (!g) return set_error(DPG_ERR_INVALID_ARG, "null graph");
+    if (!h_out && g->V > 0) return set_error(DPG_ERR_INVALID_ARG, "null output");
+    dpg_status st = DPG_OK;
+    int32_t* d = static_cast<int32_t*>(arena(c, S_LABEL, static_cast<size_t>(g->V) * 4, &st));
+    if (!d) return st;
+    DPG_TRY(run_expand(c, g, source, opts, d, bfs));
+    DPG_CUDA_TRY(cudaMemcpyAsync(h_out, d, static_cast<size_t>(g->V) * 4, cudaMemcpyDeviceToHost, c->stream));
+    return check_device(c);
+}
+
+dpg_status dpg_sssp(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_expand_opts* opts, int32_t* h_dist) {
+    return expand_host(c, g, source, opts, h_dist, false);
+}
+
+dpg_status dpg_bfs(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_expand_opts* opts, int32_t* h_level) {
+    return expand_host(c, g, source, opts, h_level, true);
+}
+
+dpg_status dpg_spmv_f32_dev(dpg_ctx* c, const dpg_graph* g, const float* d_vals, const float* d_x, float* d_y) {
+    DPG_TRY(use_device(c));
+    return run_spmv(c, const_cast<dpg_graph*>(g), d_vals, d_x, d_y);
+}
+
+dpg_status dpg_spmv_f32(dpg_ctx* c, const dpg_graph* g, const float* h_vals, const float* h_x, float* h_y) {
+    DPG_TRY(use_device(c));
+    if (!g) return set_error(DPG_ERR_INVALID_ARG, "null graph");
+    if (g->V == 0) return DPG_OK;
+    if (!h_x || !h_y || (g->E > 0 && !h_vals)) return set_error(DPG_ERR_INVALID_ARG, "null vals/x/y");
+    dpg_status st = DPG_OK;
+    const size_t nv = static_cast<size_t>(g->V), ne = static_cast<size_t>(g->E > 0 ? g->E : 1);
+    float* dv = static_cast<float*>(arena(c, S_VALS, ne * 4, &st));
+    float* dx = static_cast<float*>(arena(c, S_X, nv * 4, &st));
+    float* dy = static_cast<float*>(arena(c, S_Y, nv * 4, &st));
+    if (st != DPG_OK) return st;
+    if (g->E > 0) DPG_CUDA_TRY(cudaMemcpyAsync(dv, h_vals, static_cast<size_t>(g->E) * 4, cudaMemcpyHostToDevice, c->stream));
+    DPG_CUDA_TRY(cudaMemcpyAsync(dx, h_x, nv * 4, cudaMemcpyHostToDevice, c->stream));
+    DPG_TRY(run_spmv(c, const_cast<dpg_graph*>(g), dv, dx, dy));
+    DPG_CUDA_TRY(cudaMemcpyAsync(h_y, dy, nv * 4, cudaMemcpyDeviceToHost, c->stream));
+    return check_device(c);
+}
+
+dpg_status dpg_pagerank_f32_dev(dpg_ctx* c, const dpg_graph* g_in, const int32_t* d_outdeg, const dpg_pr_opts* opts,
+                                float* d_rank) {
+    DPG_TRY(use_device(c));
+    return run_pagerank(c, const_cast<dpg_graph*>(g_in), d_outdeg, opts, d_rank);
+}
+
+dpg_status dpg_pagerank_f32(dpg_ctx* c, const dpg_graph* g_in, const int32_t* h_outdeg, const dpg_pr_opts* opts,
+                            float* h_rank) {
+    DPG_TRY(use_device(c));
+    if (!g_in) return set_error(DPG_ERR_INVALID_ARG, "null graph");
+    if (g_in->V == 0) return DPG_OK;
+    if (!h_outdeg || !h_rank) return set_error(DPG_ERR_INVALID_ARG, "null outdeg or rank");
+    dpg_status st = DPG_OK;
+    const size_t nv = static_cast<size_t>(g_in->V);
+    int32_t* dod = static_cast<int32_t*>(arena(c, S_OUTDEG, nv * 4, &st));
+    float* dr = static_cast<float*>(arena(c, S_RANKOUT, nv * 4, &st));
+    if (st != DPG_OK) return st;
+    DPG_CUDA_TRY(cudaMemcpyAsync(dod, h_outdeg, nv * 4, cudaMemcpyHostToDevice, c->stream));
+    DPG_TRY(run_pagerank(c, const_cast<dpg_graph*>(g_in), dod, opts, dr));
+    DPG_CUDA_TRY(cudaMemcpyAsync(h_rank, dr, nv * 4, cudaMemcpyDeviceToHost, c->stream));
+    return check_device(c);
+}
+
+dpg_status dpg_sssp_host(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
+                         const int32_t* weights, int32_t source, const dpg_expand_opts* opts, int32_t* h_dist) {
+    if (!weights) return set_error(DPG_ERR_INVALID_ARG, "SSSP needs weights");
+    dpg_graph* g = nullptr;
+    DPG_TRY(dpg_graph_create(c, V, E, offsets, col, weights, &g));
+    const dpg_status s = dpg_sssp(c, g, source, opts, h_dist);
+    dpg_graph_destroy(g);
+    return s;
+}
+
+dpg_status dpg_pagerank_f32_host(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in_offsets, const int32_t* in_col,
+                                 const int32_t* outdeg, const dpg_pr_opts* opts, float* h_rank) {
+    dpg_graph* g = nullptr;
+    DPG_TRY(dpg_graph_create(c, V, E, in_offsets, in_col, nullptr, &g));
+    const dpg_status s = dpg_pagerank_f32(c, g, outdeg, opts, h_rank);
+    dpg_graph_destroy(g);
+    return s;
+}
+
+dpg_status dpg_selftest_barrier_timeout(dpg_ctx* c, double timeout_seconds) {
+    DPG_TRY(use_device(c));
+    if (!(timeout_seconds > 0) || timeout_seconds > 30) return set_error(DPG_ERR_INVALID_ARG, "timeout must be in (0, 30] s");
+    DPG_TRY(check_device(c));  // start from a clean status word
+    DPG_CUDA_TRY(launch_barrier_timeout_test(c->st, static_cast<unsigned long long>(timeout_seconds * 1e9), c->stream));
+    return check_device(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,333 @@
+// Row gathers: SpMV (y = A x over the out-edge CSR) and PageRank pull sweeps (over the in-edge CSR).
+//
+// Reference: csr_spmv_kernel (apps/SpMV/src/SpMV_kernel.cu:81-96) and pagerank_thread_pull_kernel
+// (apps/pagerank/src/pagerank_kernel.cu:95-120) map one thread to one row, so a power-law hub row
+// serialises a thread; the consolidation variants hand rows of degree >= 64 to CDP children that
+// block-reduce them (SpMV_kernel.cu:196-216, pagerank_kernel.cu:357-382).
+//
+// Here the rows are cut on the host into warp tiles of at most 256 merge items (rows + nonzeros):
+//   - a normal tile holds whole rows of degree <= 255; one warp stages the tile's row ends and
+//     gathered products in shared memory, each lane walks 8 consecutive merge items (merge-path
+//     over row ends and nonzeros), and a warp segmented scan joins rows that cross lanes;
+//   - a row of degree > 255 (a hub) is split into 256-nonzero segments whose partial sums are
+//     combined afterwards, in segment order, by the hub fix-up kernel.
+// Every sum has a fixed order, so results are bit-reproducible run to run; no float atomics.
+// PageRank folds rank/outdeg into the sweep's epilogue (contrib[v] = rank[v]/outdeg[v]), so the
+// gather reads one 4-byte value per in-edge instead of the reference's rank and outdegree pair and
+// divide per edge (pagerank_kernel.cu:114), and sums the dangling mass on the device (the reference
+// copies every dangling rank to the host each sweep, pagerank_wrapper.cu:212-218).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "dpg_kernels.h"
+
+namespace dpg {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kWarps = kBlock / 32;
+constexpr int kIpl = kRowTileItems / 32;  // merge items per lane
+constexpr int kFixBlock = 256;
+
+enum { kModeSpmv = 0, kModePagerank = 1 };
+
+template <int MODE>
+__device__ __forceinline__ float load_product(const RowGatherLaunch& L, int e) {
+    const int c = __ldg(L.col + e);
+    if (MODE == kModeSpmv) return __ldg(L.vals + e) * __ldg(L.x + c);
+    return __ldg(L.x + c);
+}
+
+// PageRank epilogue of one row: new rank, next contribution, dangling mass, convergence flag.
+__device__ __forceinline__ void pr_epilogue(const RowGatherLaunch& L, int v, float sum, float base,
+                                            double& dang) {
+    const float nv = fmaf(L.damping, sum, base);
+    if (L.rank_out) L.rank_out[v] = nv;
+    if (L.rank_prev && fabsf(nv - __ldg(L.rank_prev + v)) > L.epsilon) *L.nonstop = 1u;
+    const int od = __ldg(L.outdeg + v);
+    L.y[v] = od > 0 ? nv / static_cast<float>(od) : 0.0f;
+    if (od == 0) dang += static_cast<double>(nv);
+}
+
+__device__ __forceinline__ float pr_base(const RowGatherLaunch& L) {
+    return static_cast<float>(L.base_const + L.dangling_scale * __ldg(L.dsum_in));
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
+    __shared__ int s_re[kWarps][kRowTileItems];
+    __shared__ float s_val[kWarps][kRowTileItems];
+    __shared__ float s_out[kWarps][kRowTileItems];
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int gwarp = blockIdx.x * kWarps + warp;
+    const int nwarps = gridDim.x * kWarps;
+    int* re = s_re[warp];
+    float* val = s_val[warp];
+    float* out = s_out[warp];
+    float base = 0.0f;
+    if (MODE == kModePagerank) base = pr_base(L);
+    double dang = 0.0;
+
+    for (int t = gwarp; t < L.plan.ntiles; t += nwarps) {
+        const int4 T = __ldg(L.plan.tiles + t);
+        const int row = T.x, nrows = T.y, nb = T.z, nnz = T.w;
+        if (nrows < 0) {
+            // Hub segment: fixed-order lane sums, then a butterfly; partial goes to the fix-up.
+            float acc = 0.0f;
+#pragma unroll
+            for (int i = 0; i < kIpl; ++i) {
+                const int j = i * 32 + lane;
+                if (j < nnz) acc += load_product<MODE>(L, nb + j);
+            }
+            acc = warp_sum_f32(acc);
+            if (lane == 0) L.partial[-(nrows + 1)] = acc;
+            continue;
+        }
+        // Stage relative row ends and products.
+        for (int r = lane; r < nrows; r += 32) re[r] = __ldg(L.off + row + r + 1) - nb;
+        int cols[kIpl];
+#pragma unroll
+        for (int i = 0; i < kIpl; ++i) {
+            const int j = i * 32 + lane;
+            cols[i] = j < nnz ? __ldg(L.col + nb + j) : 0;
+        }
+#pragma unroll
+        for (int i = 0; i < kIpl; ++i) {
+            const int j = i * 32 + lane;
+            if (j < nnz) {
+                float pv = __ldg(L.x + cols[i]);
+                if (MODE == kModeSpmv) pv *= __ldg(L.vals + nb + j);
+                val[j] = pv;
+            }
+        }
+        __syncwarp();
+        // Merge-path: lane owns merge items [d0, d1). r = row ends consumed, k = nonzeros consumed.
+        const int total = nrows + nnz;
+        const int d0 = min(lane * kIpl, total);
+        const int d1 = min(d0 + kIpl, total);
+        int lo = max(0, d0 - nnz), hi = min(d0, nrows);
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (re[mid - 1] + mid <= d0) lo = mid;
+            else hi = mid - 1;
+        }
+        int r = lo, k = d0 - lo;
+        float acc = 0.0f;
+        int first_emit = -1;
+        int rend = r < nrows ? re[r] : 0x7FFFFFFF;
+        for (int it = d0; it < d1; ++it) {
+            if (k < rend) {
+                acc += val[k];
+                ++k;
+            } else {
+                if (first_emit < 0) first_emit = r;
+                out[r] = acc;
+                acc = 0.0f;
+                ++r;
+                rend = r < nrows ? re[r] : 0x7FFFFFFF;
+            }
+        }
+        // Segmented inclusive scan of the lanes' open partials (key = row still open at lane end).
+        float cv = acc;
+        const int key = r;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float tv = __shfl_up_sync(kFullMask, cv, o);
+            const int tk = __shfl_up_sync(kFullMask, key, o);
+            if (lane >= o && tk == key) cv += tv;
+        }
+        const float cin = __shfl_up_sync(kFullMask, cv, 1);
+        const int kin = __shfl_up_sync(kFullMask, key, 1);
+        if (lane > 0 && first_emit >= 0 && kin == first_emit) out[first_emit] += cin;
+        __syncwarp();
+        for (int rr = lane; rr < nrows; rr += 32) {
+            const float sum = out[rr];
+            if (MODE == kModeSpmv) {
+                L.y[row + rr] = sum;
+            } else {
+                pr_epilogue(L, row + rr, sum, base, dang);
+            }
+        }
+        __syncwarp();
+    }
+    if (MODE == kModePagerank) {
+        dang = warp_sum_f64(dang);
+        if (lane == 0) L.dpart[gwarp] = dang;
+    }
+}
+
+// Hub rows: sum the segment partials in segment order, then the row epilogue. Small hubs go one per
+// thread, big hubs one per warp. For PageRank the last CTA to finish also reduces every dangling
+// partial (gather warps, then fix-up warps, in index order) into dsum_out.
+template <int MODE>
+__global__ void __launch_bounds__(kFixBlock) hub_fixup_kernel(RowGatherLaunch L, int gather_warps, DevStatus* st) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nthreads = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    const int gwarp = tid >> 5;
+    const int nwarps = nthreads >> 5;
+    float base = 0.0f;
+    if (MODE == kModePagerank) base = pr_base(L);
+    double dang = 0.0;
+    for (int h = tid; h < L.plan.nhub_small; h += nthreads) {
+        const int4 H = __ldg(L.plan.hubs_small + h);
+        float acc = 0.0f;
+        for (int s = 0; s < H.z; ++s) acc += L.partial[H.y + s];
+        if (MODE == kModeSpmv) L.y[H.x] = acc;
+        else pr_epilogue(L, H.x, acc, base, dang);
+    }
+    for (int h = gwarp; h < L.plan.nhub_big; h += nwarps) {
+        const int4 H = __ldg(L.plan.hubs_big + h);
+        float acc = 0.0f;
+        for (int s = lane; s < H.z; s += 32) acc += L.partial[H.y + s];
+        acc = warp_sum_f32(acc);
+        if (lane == 0) {
+            if (MODE == kModeSpmv) L.y[H.x] = acc;
+            else pr_epilogue(L, H.x, acc, base, dang);
+        }
+    }
+    if (MODE != kModePagerank) return;
+    dang = warp_sum_f64(dang);
+    if (lane == 0) L.dfix[gwarp] = dang;
+    __threadfence();
+    __syncthreads();
+    __shared__ int s_last;
+    if (threadIdx.x == 0) s_last = atomicAdd(&st->fix_count, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < gather_warps; i += blockDim.x) acc += __ldcg(L.dpart + i);
+    for (int i = threadIdx.x; i < nwarps; i += blockDim.x) acc += __ldcg(L.dfix + i);
+    __shared__ double s_red[kFixBlock / 32];
+    acc = warp_sum_f64(acc);
+    if (lane == 0) s_red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double total = 0.0;
+        for (int w = 0; w < kFixBlock / 32; ++w) total += s_red[w];
+        *L.dsum_out = total;
+        st->fix_count = 0u;
+    }
+}
+
+// Initial contribution vector and its dangling mass. Uses the gather grid so dpart lines up.
+__global__ void __launch_bounds__(kBlock) pr_init_kernel(RowGatherLaunch L, float init_rank, float* rank_prev) {
+    const int lane = threadIdx.x & 31;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nthreads = gridDim.x * blockDim.x;
+    double dang = 0.0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < L.V; v += nthreads) {
+        const int od = __ldg(L.outdeg + v);
+        L.y[v] = od > 0 ? init_rank / static_cast<float>(od) : 0.0f;
+        if (rank_prev) rank_prev[v] = init_rank;
+        if (od == 0) dang += static_cast<double>(init_rank);
+    }
+    dang = warp_sum_f64(dang);
+    if (lane == 0) L.dpart[gwarp] = dang;
+}
+
+}  // namespace
+
+void rowgather_grid(int sm_count, int* gather_blocks, int* fix_blocks, int* block_threads) {
+    // 24 KB of shared memory per 256-thread CTA: up to 8 CTAs (64 warps) per SM.
+    *gather_blocks = sm_count * 8;
+    *fix_blocks = sm_count * 2;
+    *block_threads = kBlock;
+}
+
+void build_row_plan(const int32_t* off, int32_t V, RowPlanHost* plan) {
+    plan->tiles.clear();
+    plan->hubs_small.clear();
+    plan->hubs_big.clear();
+    plan->nseg = 0;
+    int32_t cur_row = 0, cur_rows = 0, cur_items = 0;
+    auto flush = [&]() {
+        if (cur_rows > 0)
+            plan->tiles.push_back(make_int4(cur_row, cur_rows, off[cur_row], off[cur_row + cur_rows] - off[cur_row]));
+        cur_rows = 0;
+        cur_items = 0;
+    };
+    for (int32_t r = 0; r < V; ++r) {
+        const int32_t d = off[r + 1] - off[r];
+        if (d > kHubRowDegree) {
+            flush();
+            const int32_t nseg = (d + kRowTileItems - 1) / kRowTileItems;
+            const int4 hub = make_int4(r, plan->nseg, nseg, 0);
+            for (int32_t s = 0; s < nseg; ++s) {
+                const int32_t b = off[r] + s * kRowTileItems;
+                plan->tiles.push_back(make_int4(r, -(plan->nseg + s + 1), b, std::min(kRowTileItems, off[r + 1] - b)));
+            }
+            plan->nseg += nseg;
+            if (nseg <= kSmallHubSegs) plan->hubs_small.push_back(hub);
+            else plan->hubs_big.push_back(hub);
+            continue;
+        }
+        if (cur_items + d + 1 > kRowTileItems) flush();
+        if (cur_rows == 0) cur_row = r;
+        ++cur_rows;
+        cur_items += d + 1;
+    }
+    flush();
+}
+
+cudaError_t launch_spmv(const RowGatherLaunch& L, DevStatus* st, cudaStream_t stream, int sm_count,
+                        LaunchHook* hook) {
+    int gb, fb, bt;
+    rowgather_grid(sm_count, &gb, &fb, &bt);
+    {
+        HookScope hs(hook, DPG_KERNEL_ROWGATHER, stream);
+        rowgather_kernel<kModeSpmv><<<gb, bt, 0, stream>>>(L);
+    }
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    if (L.plan.nhub_small + L.plan.nhub_big > 0) {
+        HookScope hs(hook, DPG_KERNEL_FIXUP, stream);
+        hub_fixup_kernel<kModeSpmv><<<fb, kFixBlock, 0, stream>>>(L, gb * (bt / 32), st);
+        err = cudaGetLastError();
+    }
+    return err;
+}
+
+cudaError_t launch_pagerank_sweep(const RowGatherLaunch& L, DevStatus* st, cudaStream_t stream, int sm_count,
+                                  LaunchHook* hook) {
+    int gb, fb, bt;
+    rowgather_grid(sm_count, &gb, &fb, &bt);
+    {
+        HookScope hs(hook, DPG_KERNEL_ROWGATHER, stream);
+        rowgather_kernel<kModePagerank><<<gb, bt, 0, stream>>>(L);
+    }
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    {
+        HookScope hs(hook, DPG_KERNEL_FIXUP, stream);
+        hub_fixup_kernel<kModePagerank><<<fb, kFixBlock, 0, stream>>>(L, gb * (bt / 32), st);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pagerank_init(const RowGatherLaunch& L, float init_rank, float* rank_prev, DevStatus* st,
+                                 cudaStream_t stream, int sm_count, LaunchHook* hook) {
+    int gb, fb, bt;
+    rowgather_grid(sm_count, &gb, &fb, &bt);
+    {
+        HookScope hs(hook, DPG_KERNEL_INIT, stream);
+        pr_init_kernel<<<gb, bt, 0, stream>>>(L, init_rank, rank_prev);
+    }
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    // A fix-up pass over no hubs reduces the initial dangling partials into dsum_out.
+    RowGatherLaunch F = L;
+    F.plan.nhub_small = 0;
+    F.plan.nhub_big = 0;
+    {
+        HookScope hs(hook, DPG_KERNEL_INIT, stream);
+        hub_fixup_kernel<kModePagerank><<<fb, kFixBlock, 0, stream>>>(F, gb * (bt / 32), st);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace dpg
