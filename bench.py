@@ -47,6 +47,9 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["dpg", "reference"], default="dpg")
     ap.add_argument("--no-extra", action="store_true", help="skip the SpMV / SSSP / BFS side measurements")
+    ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs"], default="pagerank",
+                    help="pagerank is the headline; the others print their own line (used for profiling)")
+    ap.add_argument("--scale", type=int, default=0, help="R-MAT scale for --workload spmv/sssp/bfs")
     return ap.parse_args()
 
 
@@ -188,16 +191,16 @@ def run_reference(args, world, rank):
     return 0
 
 
-def extra_measurements(dpg, ctx, torch, g, peak, steps):
-    """SpMV on the scale-22 graph; SSSP and BFS on R-MAT scale 24 (device-resident, CUDA events)."""
+def measure_spmv(dpg, ctx, torch, g, peak, steps):
+    """SpMV over the out-edge CSR with FP32 values in (0,1] and x in [-1,1]; CUDA events."""
     dev = torch.device("cuda", torch.cuda.current_device())
-    out = {}
     V, E = g.V, g.E
     rng = np.random.default_rng(22)
     vals = torch.from_numpy((1.0 - rng.random(E, dtype=np.float32)).astype(np.float32)).to(dev)
     x = torch.from_numpy(rng.uniform(-1, 1, V).astype(np.float32)).to(dev)
     y = torch.empty(V, dtype=torch.float32, device=dev)
     dg = dpg.Graph(ctx, g.offsets, g.col)
+    ctx.profile(True)
     for _ in range(3):
         dpg.spmv_dev(ctx, dg, vals.data_ptr(), x.data_ptr(), y.data_ptr())
     ctx.profile_reset()
@@ -210,43 +213,84 @@ def extra_measurements(dpg, ctx, torch, g, peak, steps):
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) / n
     lg, msg = ctx.profile_read(dpg.KERNEL_ROWGATHER)
+    gather_ms = msg / max(lg, 1)
     bytes_spmv = 4 * (V + 1) + 8 * E + 8 * V
-    out["spmv_rmat22"] = {"gteps": E / (t / 1e3) / 1e9, "ms": t, "gather_ms": msg / max(lg, 1),
-                          "roofline_frac": bytes_spmv / (msg / max(lg, 1) / 1e3) / 1e9 / peak,
-                          "bytes_per_launch": bytes_spmv}
-    del dg, vals, x, y
+    return {"gteps": E / (t / 1e3) / 1e9, "ms": t, "gather_ms": gather_ms,
+            "roofline_frac": bytes_spmv / (gather_ms / 1e3) / 1e9 / peak, "bytes_per_launch": bytes_spmv}
 
-    g24 = dpg.rmat_csr(24, 16, seed=24, wmin=1, wmax=255)
-    V24, E24 = g24.V, g24.E
-    dg24 = dpg.Graph(ctx, g24.offsets, g24.col, g24.weights)
-    deg = np.diff(g24.offsets)
-    srcs = [int(s) for s in np.random.default_rng(24).choice(np.flatnonzero(deg > 0), 4, replace=False)]
-    label = torch.empty(V24, dtype=torch.int32, device=dev)
-    for name, fn, bytes_pass in (("sssp_rmat24", dpg.sssp_dev, 4 * (V24 + 1) + 8 * E24 + 8 * V24),
-                                 ("bfs_rmat24", dpg.bfs_dev, 4 * (V24 + 1) + 4 * E24 + 8 * V24)):
-        fn(ctx, dg24, srcs[0], label.data_ptr())
+
+def measure_expand(dpg, ctx, torch, g, peak, kind, nsrc=4, seed=24):
+    """SSSP or BFS from seeded random sources with out-degree > 0; CUDA events around each solve."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    V, E = g.V, g.E
+    dg = dpg.Graph(ctx, g.offsets, g.col, g.weights)
+    deg = np.diff(g.offsets)
+    srcs = [int(s) for s in np.random.default_rng(seed).choice(np.flatnonzero(deg > 0), nsrc, replace=False)]
+    label = torch.empty(V, dtype=torch.int32, device=dev)
+    fn = dpg.sssp_dev if kind == "sssp" else dpg.bfs_dev
+    bytes_pass = 4 * (V + 1) + (8 if kind == "sssp" else 4) * E + 8 * V
+    ctx.profile(True)
+    fn(ctx, dg, srcs[0], label.data_ptr())
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times, kms, scanned, iters = [], [], [], []
+    for s in srcs:
+        ctx.profile_reset()
+        e0.record()
+        fn(ctx, dg, s, label.data_ptr())
+        e1.record()
+        torch.cuda.synchronize()
         ctx.synchronize()
-        times, kms, scanned, iters = [], [], [], []
-        for s in srcs:
-            ctx.profile_reset()
-            e0.record()
-            fn(ctx, dg24, s, label.data_ptr())
-            e1.record()
-            torch.cuda.synchronize()
-            ctx.synchronize()
-            times.append(e0.elapsed_time(e1))
-            _, km = ctx.profile_read(dpg.KERNEL_EXPAND)
-            kms.append(km)
-            st = ctx.last_stats()
-            scanned.append(st.edges_scanned / E24)
-            iters.append(st.iterations)
-        t = statistics.median(times)
-        km = statistics.median(kms)
-        out[name] = {"gteps": E24 / (t / 1e3) / 1e9, "ms": t, "kernel_ms": km,
-                     "roofline_frac": bytes_pass / (km / 1e3) / 1e9 / peak, "bytes_per_solve": bytes_pass,
-                     "edges_scanned_over_E": statistics.median(scanned), "iterations": statistics.median(iters),
-                     "sources": srcs}
+        times.append(e0.elapsed_time(e1))
+        _, km = ctx.profile_read(dpg.KERNEL_EXPAND)
+        kms.append(km)
+        st = ctx.last_stats()
+        scanned.append(st.edges_scanned / E)
+        iters.append(st.iterations)
+    t = statistics.median(times)
+    km = statistics.median(kms)
+    return {"gteps": E / (t / 1e3) / 1e9, "ms": t, "kernel_ms": km,
+            "roofline_frac": bytes_pass / (km / 1e3) / 1e9 / peak, "bytes_per_solve": bytes_pass,
+            "edges_scanned_over_E": statistics.median(scanned), "iterations": statistics.median(iters),
+            "sources": srcs}
+
+
+def extra_measurements(dpg, ctx, torch, g, peak, steps):
+    """SpMV on the scale-22 graph; SSSP and BFS on R-MAT scale 24 (device-resident, CUDA events)."""
+    out = {"spmv_rmat22": measure_spmv(dpg, ctx, torch, g, peak, steps)}
+    g24 = dpg.rmat_csr(24, 16, seed=24, wmin=1, wmax=255)
+    out["sssp_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "sssp")
+    out["bfs_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "bfs")
     return out
+
+
+def run_single_workload(args):
+    """--workload spmv|sssp|bfs: one measurement, one JSON line (profiling entry point)."""
+    import torch
+
+    import __graft_entry__
+
+    dpg = __graft_entry__.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    peak, peak_kind = measured_peaks()
+    ctx = dpg.Context(0)
+    ctx.set_stream(stream.cuda_stream)
+    if args.workload == "spmv":
+        scale = args.scale or 22
+        g = dpg.rmat_csr(scale, 16, seed=scale, weights=False)
+        res = measure_spmv(dpg, ctx, torch, g, peak, args.steps)
+    else:
+        scale = args.scale or 24
+        g = dpg.rmat_csr(scale, 16, seed=scale, wmin=1, wmax=255)
+        res = measure_expand(dpg, ctx, torch, g, peak, args.workload)
+    line = {"metric": f"GTEPS ({args.workload})", "value": res["gteps"], "unit": "GTEPS", "n_gpus": 1,
+            "config": {"workload": f"{args.workload} rmat scale {scale} edge-factor 16", "vertices": g.V,
+                       "arcs": g.E}, "peak_source": peak_kind, **res}
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def run_dpg(args, world, rank, local):
@@ -257,6 +301,9 @@ def run_dpg(args, world, rank, local):
     dpg = __graft_entry__.load_package()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    # One dedicated stream for the library launches and the timing events.
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     if world > 1:
         import torch.distributed as tdist
 
@@ -266,7 +313,7 @@ def run_dpg(args, world, rank, local):
     g, in_off, in_col, od = build_workload(dpg)
     V, E = g.V, g.E
     ctx = dpg.Context(local)
-    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    ctx.set_stream(stream.cuda_stream)
     gi = dpg.Graph(ctx, in_off, in_col)
     od_t = torch.from_numpy(od).to(dev)
     rank_t = torch.empty(V, dtype=torch.float32, device=dev)
@@ -374,6 +421,8 @@ def main() -> int:
     world, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    if args.workload != "pagerank":
+        return run_single_workload(args)
     return run_dpg(args, world, rank, local)
 
 

@@ -22,6 +22,12 @@
  *   oracle_pagerank_omp_f32   OpenMP FP32 pull PageRank (timed CPU baseline).
  *   oracle_color              gclr_bitmap_kernel rounds (apps/graph-color/src/graph_color_kernel.cu:28-49,
  *                             graph_color_wrapper.cu:113-130).
+ *
+ * Pinning: oracle_bfs is checked against the reference's own bfs_cpu (compiled into
+ * oracle/_ref/libref.so, recorded in tests/golden/); oracle_sssp_* against the known distances of the
+ * reference's datasets/data_test.gr and against each other. SpMV and PageRank: parity unpinned by the
+ * reference, which has no CPU implementation of them; they are restated from the kernel sources and
+ * checked in the reference's exact FP64 known-answer mode (data[e] = e%13+0.5, x[i] = i%17+0.5).
  */
 #include <math.h>
 #include <stdint.h>

@@ -334,7 +334,15 @@ class Context:
             pass
 
     def set_stream(self, stream_handle: int | None) -> None:
-        _check(lib().dpg_ctx_set_stream(self.handle, c_void_p(stream_handle) if stream_handle else None))
+        """Runs later calls on a cudaStream_t handle. None restores the context's own stream; 0 (what
+        torch reports for the default stream) selects the legacy default stream (cudaStreamLegacy)."""
+        if stream_handle is None:
+            h = None
+        elif stream_handle == 0:
+            h = c_void_p(1)  # cudaStreamLegacy
+        else:
+            h = c_void_p(stream_handle)
+        _check(lib().dpg_ctx_set_stream(self.handle, h))
 
     def synchronize(self) -> None:
         _check(lib().dpg_ctx_synchronize(self.handle))

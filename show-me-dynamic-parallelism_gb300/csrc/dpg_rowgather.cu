@@ -30,6 +30,10 @@ constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
 constexpr int kIpl = kRowTileItems / 32;  // merge items per lane
 constexpr int kFixBlock = 256;
+// Shared-memory index with one pad word per 32: lane l walking items 8l.. then hits 32 distinct banks
+// instead of 4 (an 8-way conflict without the pad).
+constexpr int kPadded = kRowTileItems + kRowTileItems / 32;
+__device__ __forceinline__ int pad(int i) { return i + (i >> 5); }
 
 enum { kModeSpmv = 0, kModePagerank = 1 };
 
@@ -57,9 +61,9 @@ __device__ __forceinline__ float pr_base(const RowGatherLaunch& L) {
 
 template <int MODE>
 __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
-    __shared__ int s_re[kWarps][kRowTileItems];
-    __shared__ float s_val[kWarps][kRowTileItems];
-    __shared__ float s_out[kWarps][kRowTileItems];
+    __shared__ int s_re[kWarps][kPadded];
+    __shared__ float s_val[kWarps][kPadded];
+    __shared__ float s_out[kWarps][kPadded];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int gwarp = blockIdx.x * kWarps + warp;
@@ -87,7 +91,7 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
             continue;
         }
         // Stage relative row ends and products.
-        for (int r = lane; r < nrows; r += 32) re[r] = __ldg(L.off + row + r + 1) - nb;
+        for (int r = lane; r < nrows; r += 32) re[pad(r)] = __ldg(L.off + row + r + 1) - nb;
         int cols[kIpl];
 #pragma unroll
         for (int i = 0; i < kIpl; ++i) {
@@ -100,7 +104,7 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
             if (j < nnz) {
                 float pv = __ldg(L.x + cols[i]);
                 if (MODE == kModeSpmv) pv *= __ldg(L.vals + nb + j);
-                val[j] = pv;
+                val[pad(j)] = pv;
             }
         }
         __syncwarp();
@@ -111,23 +115,26 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
         int lo = max(0, d0 - nnz), hi = min(d0, nrows);
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (re[mid - 1] + mid <= d0) lo = mid;
+            if (re[pad(mid - 1)] + mid <= d0) lo = mid;
             else hi = mid - 1;
         }
         int r = lo, k = d0 - lo;
         float acc = 0.0f;
         int first_emit = -1;
-        int rend = r < nrows ? re[r] : 0x7FFFFFFF;
-        for (int it = d0; it < d1; ++it) {
-            if (k < rend) {
-                acc += val[k];
-                ++k;
-            } else {
-                if (first_emit < 0) first_emit = r;
-                out[r] = acc;
-                acc = 0.0f;
-                ++r;
-                rend = r < nrows ? re[r] : 0x7FFFFFFF;
+        int rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
+#pragma unroll
+        for (int i = 0; i < kIpl; ++i) {
+            if (d0 + i < d1) {
+                if (k < rend) {
+                    acc += val[pad(k)];
+                    ++k;
+                } else {
+                    if (first_emit < 0) first_emit = r;
+                    out[pad(r)] = acc;
+                    acc = 0.0f;
+                    ++r;
+                    rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
+                }
             }
         }
         // Segmented inclusive scan of the lanes' open partials (key = row still open at lane end).
@@ -141,10 +148,10 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
         }
         const float cin = __shfl_up_sync(kFullMask, cv, 1);
         const int kin = __shfl_up_sync(kFullMask, key, 1);
-        if (lane > 0 && first_emit >= 0 && kin == first_emit) out[first_emit] += cin;
+        if (lane > 0 && first_emit >= 0 && kin == first_emit) out[pad(first_emit)] += cin;
         __syncwarp();
         for (int rr = lane; rr < nrows; rr += 32) {
-            const float sum = out[rr];
+            const float sum = out[pad(rr)];
             if (MODE == kModeSpmv) {
                 L.y[row + rr] = sum;
             } else {
@@ -233,7 +240,7 @@ __global__ void __launch_bounds__(kBlock) pr_init_kernel(RowGatherLaunch L, floa
 }  // namespace
 
 void rowgather_grid(int sm_count, int* gather_blocks, int* fix_blocks, int* block_threads) {
-    // 24 KB of shared memory per 256-thread CTA: up to 8 CTAs (64 warps) per SM.
+    // 24.75 KB of shared memory per 256-thread CTA: up to 8 CTAs (64 warps) per SM.
     *gather_blocks = sm_count * 8;
     *fix_blocks = sm_count * 2;
     *block_threads = kBlock;
