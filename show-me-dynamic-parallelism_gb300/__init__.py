@@ -136,6 +136,7 @@ _SIGS = {
     "dpg_sssp_host": [_P, c_int32, c_int64, _P, _P, _P, c_int32, POINTER(ExpandOpts), _P],
     "dpg_pagerank_f32_host": [_P, c_int32, c_int64, _P, _P, _P, POINTER(PrOpts), _P],
     "dpg_selftest_barrier_timeout": [_P, c_double],
+    "dpg_sssp_noalloc_dev": [c_int32, c_int64, _P, _P, c_int32, _P, _P],
     "dpg_read_graph": [c_char_p, c_int32, POINTER(_HostGraph)],
     "dpg_host_graph_free": [POINTER(_HostGraph)],
     "dpg_csr_from_arcs": [c_int32, c_int64, _P, _P, _P, _P, _P, _P],
@@ -489,6 +490,18 @@ def pagerank_host(ctx: Context, in_offsets, in_col, outdeg, out=None, **opts) ->
     _check(lib().dpg_pagerank_f32_host(ctx.handle, V, int(ic.shape[0]), _ptr(io), _ptr(ic), _ptr(od), byref(o),
                                        _ptr(r)))
     return r[:V]
+
+
+NOALLOC_MAX_VERTICES = 1 << 18
+NOALLOC_MAX_ARCS = 1 << 22
+
+
+def sssp_noalloc_dev(V: int, E: int, d_offsets: int, d_adj_pairs: int, source: int, d_dist: int,
+                     stream: int = 0) -> None:
+    """SSSP that allocates nothing (see include/dpg.h): device pointers in and out, workspace in a
+    fixed array inside the library; synchronises `stream`."""
+    _check(lib().dpg_sssp_noalloc_dev(V, E, c_void_p(d_offsets), c_void_p(d_adj_pairs), source, c_void_p(d_dist),
+                                      c_void_p(stream) if stream else None))
 
 
 def selftest_barrier_timeout(ctx: Context, seconds: float = 0.5) -> int:
