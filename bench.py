@@ -50,6 +50,7 @@ def parse_args():
     ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs"], default="pagerank",
                     help="pagerank is the headline; the others print their own line (used for profiling)")
     ap.add_argument("--scale", type=int, default=0, help="R-MAT scale for --workload spmv/sssp/bfs")
+    ap.add_argument("--no-relabel", action="store_true", help="turn off the column renaming of SpMV/PageRank")
     return ap.parse_args()
 
 
@@ -191,7 +192,7 @@ def run_reference(args, world, rank):
     return 0
 
 
-def measure_spmv(dpg, ctx, torch, g, peak, steps):
+def measure_spmv(dpg, ctx, torch, g, peak, steps, relabel=True):
     """SpMV over the out-edge CSR with FP32 values in (0,1] and x in [-1,1]; CUDA events."""
     dev = torch.device("cuda", torch.cuda.current_device())
     V, E = g.V, g.E
@@ -200,6 +201,7 @@ def measure_spmv(dpg, ctx, torch, g, peak, steps):
     x = torch.from_numpy(rng.uniform(-1, 1, V).astype(np.float32)).to(dev)
     y = torch.empty(V, dtype=torch.float32, device=dev)
     dg = dpg.Graph(ctx, g.offsets, g.col)
+    dg.set_relabel(relabel)
     ctx.profile(True)
     for _ in range(3):
         dpg.spmv_dev(ctx, dg, vals.data_ptr(), x.data_ptr(), y.data_ptr())
@@ -247,9 +249,14 @@ def measure_expand(dpg, ctx, torch, g, peak, kind, nsrc=4, seed=24):
         st = ctx.last_stats()
         scanned.append(st.edges_scanned / E)
         iters.append(st.iterations)
+    ctx.trace(100000)
+    fn(ctx, dg, srcs[0], label.data_ptr())
+    tr = ctx.trace_read()
+    ctx.trace(0)
+    trace = [[round((tr[i + 1, 0] - tr[i, 0]) / 1e3, 1), int(tr[i, 1]), int(tr[i, 2])] for i in range(len(tr) - 1)]
     t = statistics.median(times)
     km = statistics.median(kms)
-    return {"gteps": E / (t / 1e3) / 1e9, "ms": t, "kernel_ms": km,
+    return {"gteps": E / (t / 1e3) / 1e9, "ms": t, "kernel_ms": km, "trace_us_small_chunks": trace,
             "roofline_frac": bytes_pass / (km / 1e3) / 1e9 / peak, "bytes_per_solve": bytes_pass,
             "edges_scanned_over_E": statistics.median(scanned), "iterations": statistics.median(iters),
             "sources": srcs}
@@ -281,7 +288,7 @@ def run_single_workload(args):
     if args.workload == "spmv":
         scale = args.scale or 22
         g = dpg.rmat_csr(scale, 16, seed=scale, weights=False)
-        res = measure_spmv(dpg, ctx, torch, g, peak, args.steps)
+        res = measure_spmv(dpg, ctx, torch, g, peak, args.steps, relabel=not args.no_relabel)
     else:
         scale = args.scale or 24
         g = dpg.rmat_csr(scale, 16, seed=scale, wmin=1, wmax=255)
@@ -315,6 +322,7 @@ def run_dpg(args, world, rank, local):
     ctx = dpg.Context(local)
     ctx.set_stream(stream.cuda_stream)
     gi = dpg.Graph(ctx, in_off, in_col)
+    gi.set_relabel(not args.no_relabel)
     od_t = torch.from_numpy(od).to(dev)
     rank_t = torch.empty(V, dtype=torch.float32, device=dev)
     for _ in range(max(args.warmup, 3)):

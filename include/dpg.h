@@ -115,6 +115,11 @@ dpg_status dpg_graph_create(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* o
 dpg_status dpg_graph_create_device(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* d_offsets,
                                    const int32_t* d_col, const int32_t* d_weights, dpg_graph** out);
 dpg_status dpg_graph_destroy(dpg_graph* g);
+/* Gather-locality layout for SpMV / PageRank (on by default): column ids are renamed once, by
+ * descending frequency, so hot gathered values share cache sectors. Rows and the order of nonzeros in
+ * each row are unchanged, so results are bit-identical either way; enable = 0 turns it off. No
+ * counterpart in the reference. */
+dpg_status dpg_graph_relabel(dpg_graph* g, int32_t enable);
 dpg_status dpg_graph_info(const dpg_graph* g, int32_t* V, int64_t* E, int32_t* weighted);
 
 /* ---- SSSP (replaces SSSP_GPU, apps/sssp/src/sssp_wrapper.cu:304-341) --------------------------- */
@@ -186,6 +191,13 @@ dpg_status dpg_ctx_profile_enable(dpg_ctx* ctx, int32_t enable);
 dpg_status dpg_ctx_profile_reset(dpg_ctx* ctx);
 /* Synchronises; launches and summed event time (ms) of one kind since the last reset. */
 dpg_status dpg_ctx_profile_read(dpg_ctx* ctx, int32_t kind, int64_t* launches, double* total_ms);
+
+/* Per-iteration trace of the SSSP/BFS persistent kernel: max_iterations > 0 records, for each
+ * frontier iteration j, {global ns at its start, small-frontier length, chunk count, 0}, then an end
+ * entry {ns, 0, 0, 1}; 0 turns it off. dpg_ctx_trace_read copies up to `capacity` entries of
+ * 4 int64 each (synchronises) and reports how many slots exist. */
+dpg_status dpg_ctx_trace_enable(dpg_ctx* ctx, int32_t max_iterations);
+dpg_status dpg_ctx_trace_read(dpg_ctx* ctx, int64_t* out, int32_t capacity, int32_t* count);
 
 /* ---- failure-detection self test --------------------------------------------------------------- */
 /* Runs the persistent kernel's grid barrier with one block missing, so its bounded wait must run

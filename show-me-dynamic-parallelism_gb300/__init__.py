@@ -121,9 +121,12 @@ _SIGS = {
     "dpg_ctx_profile_enable": [_P, c_int32],
     "dpg_ctx_profile_reset": [_P],
     "dpg_ctx_profile_read": [_P, c_int32, POINTER(c_int64), POINTER(c_double)],
+    "dpg_ctx_trace_enable": [_P, c_int32],
+    "dpg_ctx_trace_read": [_P, _P, c_int32, POINTER(c_int32)],
     "dpg_graph_create": [_P, c_int32, c_int64, _P, _P, _P, POINTER(_P)],
     "dpg_graph_create_device": [_P, c_int32, c_int64, _P, _P, _P, POINTER(_P)],
     "dpg_graph_destroy": [_P],
+    "dpg_graph_relabel": [_P, c_int32],
     "dpg_graph_info": [_P, POINTER(c_int32), POINTER(c_int64), POINTER(c_int32)],
     "dpg_sssp": [_P, _P, c_int32, POINTER(ExpandOpts), _P],
     "dpg_sssp_dev": [_P, _P, c_int32, POINTER(ExpandOpts), _P],
@@ -366,6 +369,19 @@ class Context:
         _check(lib().dpg_ctx_profile_read(self.handle, kind, byref(n), byref(ms)))
         return n.value, ms.value
 
+    def trace(self, max_iterations: int) -> None:
+        """Records a per-iteration trace of later SSSP/BFS solves (0 turns it off)."""
+        _check(lib().dpg_ctx_trace_enable(self.handle, max_iterations))
+
+    def trace_read(self, capacity: int = 100000) -> np.ndarray:
+        """[k, 4] int64 rows {ns at iteration start, small frontier, chunks, end flag} of the last solve."""
+        buf = np.zeros((capacity, 4), np.int64)
+        n = c_int32()
+        _check(lib().dpg_ctx_trace_read(self.handle, _ptr(buf), capacity, byref(n)))
+        rows = buf[: n.value]
+        end = np.flatnonzero(rows[:, 3] == 1)
+        return rows[: end[0] + 1] if end.size else rows[(rows[:, 0] != 0)]
+
     @property
     def sm_count(self) -> int:
         n = c_int32()
@@ -396,6 +412,10 @@ class Graph:
         _check(lib().dpg_graph_create_device(ctx.handle, V, E, c_void_p(d_offsets), c_void_p(d_col),
                                              c_void_p(d_weights) if d_weights else None, byref(h)))
         return cls(ctx, None, None, _handle=h, _V=V, _E=E)
+
+    def set_relabel(self, enable: bool) -> None:
+        """Column renaming by frequency for SpMV/PageRank (on by default; results are identical)."""
+        _check(lib().dpg_graph_relabel(self.handle, 1 if enable else 0))
 
     def close(self) -> None:
         if self.handle:

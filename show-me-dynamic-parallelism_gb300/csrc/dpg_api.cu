@@ -44,9 +44,8 @@ using namespace dpg;
 namespace dpg_api {
 
 enum Slot {
-    S_QV0, S_QV1, S_QSE0, S_QSE1, S_BMP0, S_BMP1, S_HV0, S_HV1, S_HSE0, S_HSE1, S_HCP0, S_HCP1,
-    S_HOW0, S_HOW1, S_QCOUNT, S_HCOUNT, S_LABEL, S_CONTRIB0, S_CONTRIB1, S_RANK0, S_RANK1,
-    S_PARTIAL, S_DPART, S_DFIX, S_DSUM, S_NONSTOP, S_VALS, S_X, S_Y, S_OUTDEG, S_RANKOUT,
+    S_QV0, S_QV1, S_QSE0, S_QSE1, S_BMP0, S_BMP1, S_CH0, S_CH1, S_QCOUNT, S_CCOUNT, S_LABEL, S_CONTRIB0, S_CONTRIB1, S_RANK0, S_RANK1,
+    S_PARTIAL, S_DPART, S_DFIX, S_DSUM, S_NONSTOP, S_VALS, S_X, S_Y, S_OUTDEG, S_RANKOUT, S_XPERM,
     S_COUNT_SLOTS
 };
 
@@ -128,12 +127,15 @@ struct dpg_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     int sm_count = 0;
+    int smem_optin = 0;  // max dynamic shared memory per CTA (bytes)
     DevStatus* st = nullptr;
     Buf bufs[S_COUNT_SLOTS];
     int last_grid = 0;
     int last_block = 0;
     int64_t last_host_iterations = -1;  // PageRank sweeps (host-counted); -1: read from the device
     Profiler prof;
+    unsigned long long* trace = nullptr;  // per-iteration expansion trace (dpg_ctx_trace_enable)
+    int32_t trace_cap = 0;
 };
 
 struct dpg_graph {
@@ -148,6 +150,12 @@ struct dpg_graph {
     int32_t max_degree = 0;
     bool plan_ready = false;
     RowPlanDev plan;
+    // Column renaming by frequency for the row gathers (dpg_layout.cu); built on first use.
+    bool relabel = true;
+    bool relabel_ready = false;
+    int32_t* perm = nullptr;  // old column id -> new
+    int32_t* inv = nullptr;   // new -> old
+    int32_t* pcol = nullptr;  // col[e] renamed
 };
 
 namespace dpg_api {
@@ -241,6 +249,11 @@ void graph_free_device(dpg_graph* g) {
     cudaFree(g->off);
     cudaFree(g->col);
     cudaFree(g->adj);
+    cudaFree(g->perm);
+    cudaFree(g->inv);
+    cudaFree(g->pcol);
+    g->perm = g->inv = g->pcol = nullptr;
+    g->relabel_ready = false;
     cudaFree(g->plan.tiles);
     cudaFree(g->plan.hubs_small);
     cudaFree(g->plan.hubs_big);
@@ -277,6 +290,42 @@ dpg_status ensure_plan(dpg_graph* g) {
     return DPG_OK;
 }
 
+// Builds perm/inv/pcol for the row gathers: column counts on the device, the frequency order on
+// the host (a 33-bucket stable multi-split), the renamed column array on the device.
+// Entries of the gathered vector kept in shared memory by the row-gather kernel: as many of the
+// most frequent (renamed) columns as fit next to the tile staging.
+int32_t hot_entries(const dpg_ctx* c, const dpg_graph* g) {
+    if (!g->relabel) return 0;
+    const int64_t room = static_cast<int64_t>(c->smem_optin) - static_cast<int64_t>(rowgather_staging_bytes()) - 1024;
+    const int64_t cap = room > 0 ? room / 4 : 0;
+    return static_cast<int32_t>(cap < g->V ? cap : g->V);
+}
+
+dpg_status ensure_relabel(dpg_graph* g) {
+    if (g->relabel_ready || g->V == 0) return DPG_OK;
+    dpg_ctx* c = g->ctx;
+    const size_t nv = static_cast<size_t>(g->V);
+    int32_t* counts = nullptr;
+    DPG_CUDA_TRY(cudaMalloc(&counts, nv * 4));
+    std::vector<int32_t> h_counts(nv), h_perm(nv), h_inv(nv);
+    cudaError_t e = cudaMemsetAsync(counts, 0, nv * 4, c->stream);
+    if (e == cudaSuccess) e = launch_column_histogram(g->col, g->E, counts, c->stream, c->sm_count);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_counts.data(), counts, nv * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(counts);
+    if (e != cudaSuccess) return set_error(DPG_ERR_CUDA, std::string("column histogram: ") + cudaGetErrorString(e));
+    frequency_order(h_counts.data(), g->V, h_perm.data(), h_inv.data());
+    DPG_CUDA_TRY(cudaMalloc(&g->perm, nv * 4));
+    DPG_CUDA_TRY(cudaMalloc(&g->inv, nv * 4));
+    DPG_CUDA_TRY(cudaMalloc(&g->pcol, static_cast<size_t>(g->E > 0 ? g->E : 1) * 4));
+    DPG_CUDA_TRY(cudaMemcpyAsync(g->perm, h_perm.data(), nv * 4, cudaMemcpyHostToDevice, c->stream));
+    DPG_CUDA_TRY(cudaMemcpyAsync(g->inv, h_inv.data(), nv * 4, cudaMemcpyHostToDevice, c->stream));
+    DPG_CUDA_TRY(launch_relabel_columns(g->col, g->perm, g->E, g->pcol, c->stream, c->sm_count));
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    g->relabel_ready = true;
+    return DPG_OK;
+}
+
 void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const dpg_graph* g) {
     if (in) *o = *in;
     else {
@@ -284,7 +333,7 @@ void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const d
         o->solution = DPG_SOL_BINNED;
     }
     if (o->threshold <= 0) o->threshold = DPG_REF_THRESHOLD;
-    if (o->hub_threshold <= 0) o->hub_threshold = 1024;
+    if (o->hub_threshold <= 0) o->hub_threshold = 32;
     if (o->solution == DPG_SOL_GRID) o->hub_threshold = o->threshold;
     if (o->max_iterations <= 0) {
         const int64_t cap = static_cast<int64_t>(g->V) + 2;
@@ -303,11 +352,11 @@ dpg_status run_expand(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_
     fill_expand_defaults(in_opts, &o, g);
     if (o.solution < DPG_SOL_THREAD || o.solution > DPG_SOL_BINNED)
         return set_error(DPG_ERR_INVALID_ARG, "unknown solution id");
-    const int32_t min_hub = (o.solution == DPG_SOL_GRID) ? o.threshold : o.hub_threshold;
+    const int32_t min_chunked = (o.solution == DPG_SOL_GRID) ? o.threshold : o.hub_threshold;
     ExpandWorkspace ws;
     memset(&ws, 0, sizeof(ws));
     ws.cap_v = static_cast<int64_t>(g->V) + 1;
-    expand_workspace_caps(g->V, g->E, min_hub, &ws.cap_hub, &ws.cap_chunks);
+    ws.cap_chunks = expand_chunk_capacity(g->V, g->E, min_chunked);
     ws.bmp_words = (g->V + 31) / 32 + 1;
     dpg_status st = DPG_OK;
     const size_t nv = static_cast<size_t>(ws.cap_v);
@@ -317,17 +366,11 @@ dpg_status run_expand(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_
     ws.qse[1] = static_cast<int2*>(arena(c, S_QSE1, nv * 8, &st));
     ws.bmp[0] = static_cast<uint32_t*>(arena(c, S_BMP0, static_cast<size_t>(ws.bmp_words) * 4, &st));
     ws.bmp[1] = static_cast<uint32_t*>(arena(c, S_BMP1, static_cast<size_t>(ws.bmp_words) * 4, &st));
-    const size_t nh = static_cast<size_t>(ws.cap_hub), nc = static_cast<size_t>(ws.cap_chunks);
-    ws.hv[0] = static_cast<int32_t*>(arena(c, S_HV0, nh * 4, &st));
-    ws.hv[1] = static_cast<int32_t*>(arena(c, S_HV1, nh * 4, &st));
-    ws.hse[0] = static_cast<int2*>(arena(c, S_HSE0, nh * 8, &st));
-    ws.hse[1] = static_cast<int2*>(arena(c, S_HSE1, nh * 8, &st));
-    ws.hcpos[0] = static_cast<int32_t*>(arena(c, S_HCP0, nh * 4, &st));
-    ws.hcpos[1] = static_cast<int32_t*>(arena(c, S_HCP1, nh * 4, &st));
-    ws.howner[0] = static_cast<int32_t*>(arena(c, S_HOW0, nc * 4, &st));
-    ws.howner[1] = static_cast<int32_t*>(arena(c, S_HOW1, nc * 4, &st));
+    const size_t nc = static_cast<size_t>(ws.cap_chunks);
+    ws.chunks[0] = static_cast<int4*>(arena(c, S_CH0, nc * 16, &st));
+    ws.chunks[1] = static_cast<int4*>(arena(c, S_CH1, nc * 16, &st));
     ws.qcount = static_cast<uint32_t*>(arena(c, S_QCOUNT, 4 * 4, &st));
-    ws.hcount = static_cast<unsigned long long*>(arena(c, S_HCOUNT, 4 * 8, &st));
+    ws.ccount = static_cast<uint32_t*>(arena(c, S_CCOUNT, 4 * 4, &st));
     if (st != DPG_OK) return st;
     ExpandLaunch L;
     L.off = g->off;
@@ -343,6 +386,9 @@ dpg_status run_expand(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_
     L.hub_threshold = o.hub_threshold;
     L.max_iter = o.max_iterations;
     L.timeout_ns = static_cast<unsigned long long>(o.timeout_seconds * 1e9);
+    L.trace = c->trace;
+    L.trace_cap = c->trace_cap;
+    if (c->trace) DPG_CUDA_TRY(cudaMemsetAsync(c->trace, 0, sizeof(unsigned long long) * 4 * c->trace_cap, c->stream));
     c->last_host_iterations = -1;
     DPG_CUDA_TRY(launch_expand(L, ws, c->st, c->stream, c->sm_count, &c->last_grid, &c->last_block, &c->prof));
     return DPG_OK;
@@ -370,6 +416,7 @@ dpg_status run_pagerank(dpg_ctx* c, dpg_graph* g, const int32_t* d_outdeg, const
     DPG_TRY(pr_defaults(in_opts, &o));
     if (g->V == 0) return DPG_OK;
     DPG_TRY(ensure_plan(g));
+    if (g->relabel) DPG_TRY(ensure_relabel(g));
     int gb, fb, bt;
     rowgather_grid(c->sm_count, &gb, &fb, &bt);
     dpg_status st = DPG_OK;
@@ -392,7 +439,9 @@ dpg_status run_pagerank(dpg_ctx* c, dpg_graph* g, const int32_t* d_outdeg, const
     memset(&L, 0, sizeof(L));
     L.plan = g->plan;
     L.off = g->off;
-    L.col = g->col;
+    L.col = g->relabel ? g->pcol : g->col;
+    L.perm = g->relabel ? g->perm : nullptr;
+    L.hot = hot_entries(c, g);
     L.vals = nullptr;
     L.partial = partial;
     L.V = g->V;
@@ -404,6 +453,10 @@ dpg_status run_pagerank(dpg_ctx* c, dpg_graph* g, const int32_t* d_outdeg, const
     L.dfix = dfix;
     L.epsilon = static_cast<float>(o.epsilon);
     const float init_rank = o.init_zero ? 0.0f : static_cast<float>(o.total_rank / static_cast<double>(g->V));
+    // Contributions of vertices without out-arcs are never written by a sweep; start them at 0 so
+    // an out-degree array that disagrees with the graph still reads defined values.
+    DPG_CUDA_TRY(cudaMemsetAsync(contrib[0], 0, nv * 4, c->stream));
+    DPG_CUDA_TRY(cudaMemsetAsync(contrib[1], 0, nv * 4, c->stream));
     // Initial vector: contributions into contrib[0], dangling mass into dsum[0].
     L.y = contrib[0];
     L.dsum_in = dsum + 1;
@@ -450,16 +503,20 @@ dpg_status run_spmv(dpg_ctx* c, dpg_graph* g, const float* d_vals, const float* 
     if (g->V == 0) return DPG_OK;
     if (!d_x || !d_y || (g->E > 0 && !d_vals)) return set_error(DPG_ERR_INVALID_ARG, "null vals/x/y");
     DPG_TRY(ensure_plan(g));
+    if (g->relabel) DPG_TRY(ensure_relabel(g));
     dpg_status st = DPG_OK;
     float* partial = static_cast<float*>(arena(c, S_PARTIAL, static_cast<size_t>(g->plan.nseg + 1) * 4, &st));
+    float* xp = g->relabel ? static_cast<float*>(arena(c, S_XPERM, static_cast<size_t>(g->V) * 4, &st)) : nullptr;
     if (st != DPG_OK) return st;
+    if (xp) DPG_CUDA_TRY(launch_gather_by_index(d_x, g->inv, g->V, xp, c->stream, c->sm_count));
     RowGatherLaunch L;
     memset(&L, 0, sizeof(L));
     L.plan = g->plan;
     L.off = g->off;
-    L.col = g->col;
+    L.col = g->relabel ? g->pcol : g->col;
     L.vals = d_vals;
-    L.x = d_x;
+    L.x = xp ? xp : d_x;
+    L.hot = hot_entries(c, g);
     L.y = d_y;
     L.partial = partial;
     L.V = g->V;
@@ -560,6 +617,7 @@ dpg_status dpg_ctx_create(int device, dpg_ctx** out) {
     c->device = device;
     cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (e == cudaSuccess) e = cudaMalloc(&c->st, sizeof(DevStatus));
     if (e == cudaSuccess) e = cudaMemset(c->st, 0, sizeof(DevStatus));
     if (e != cudaSuccess) {
@@ -579,6 +637,7 @@ dpg_status dpg_ctx_destroy(dpg_ctx* c) {
     cudaStreamSynchronize(c->stream);
     for (auto& b : c->bufs) cudaFree(b.p);
     cudaFree(c->st);
+    cudaFree(c->trace);
     cudaStreamDestroy(c->own_stream);
     delete c;
     return DPG_OK;
@@ -632,6 +691,30 @@ dpg_status dpg_ctx_profile_read(dpg_ctx* c, int32_t kind, int64_t* launches, dou
     return DPG_OK;
 }
 
+dpg_status dpg_ctx_trace_enable(dpg_ctx* c, int32_t max_iterations) {
+    DPG_TRY(use_device(c));
+    if (max_iterations < 0) return set_error(DPG_ERR_INVALID_ARG, "max_iterations must be >= 0");
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    cudaFree(c->trace);
+    c->trace = nullptr;
+    c->trace_cap = 0;
+    if (max_iterations > 0) {
+        DPG_CUDA_TRY(cudaMalloc(&c->trace, sizeof(unsigned long long) * 4 * (static_cast<size_t>(max_iterations) + 1)));
+        c->trace_cap = max_iterations + 1;
+    }
+    return DPG_OK;
+}
+
+dpg_status dpg_ctx_trace_read(dpg_ctx* c, int64_t* out, int32_t capacity, int32_t* count) {
+    DPG_TRY(use_device(c));
+    if (!out || !count || capacity < 0) return set_error(DPG_ERR_INVALID_ARG, "null output");
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const int32_t n = capacity < c->trace_cap ? capacity : c->trace_cap;
+    if (n > 0) DPG_CUDA_TRY(cudaMemcpy(out, c->trace, sizeof(int64_t) * 4 * n, cudaMemcpyDeviceToHost));
+    *count = n;
+    return DPG_OK;
+}
+
 dpg_status dpg_ctx_sm_count(dpg_ctx* c, int32_t* out) {
     if (!c || !out) return set_error(DPG_ERR_INVALID_ARG, "null argument");
     *out = c->sm_count;
@@ -654,6 +737,12 @@ dpg_status dpg_graph_destroy(dpg_graph* g) {
     cudaStreamSynchronize(g->ctx->stream);
     graph_free_device(g);
     delete g;
+    return DPG_OK;
+}
+
+dpg_status dpg_graph_relabel(dpg_graph* g, int32_t enable) {
+    if (!g) return set_error(DPG_ERR_INVALID_ARG, "null graph");
+    g->relabel = enable != 0;
     return DPG_OK;
 }
 

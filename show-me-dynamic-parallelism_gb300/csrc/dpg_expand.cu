@@ -18,8 +18,10 @@
 //   DPG_SOL_BLOCK   degree >= threshold: consolidated per CTA in shared memory and expanded by the
 //                   whole CTA                                               (-s 3)
 //   DPG_SOL_GRID    degree >= threshold: consolidated grid-wide at push time and expanded by every
-//                   warp of the grid in 256-edge chunks                      (-s 4)
-//   DPG_SOL_BINNED  warp scan-gather below the hub threshold, grid-wide chunks above (default)
+//                   warp of the grid in 256-arc chunks                       (-s 4)
+//   DPG_SOL_BINNED  binned at push time: below hub_threshold (default 32) into the small queue,
+//                   expanded by warp scan-gathers over 32 vertices; at or above it cut into 256-arc
+//                   chunks over every warp, so no work item exceeds 8 warp steps (default)
 // BFS uses the same machinery with level[v] set once by atomicCAS (bfs_rec_kernel.cu:76-78).
 
 #include <cuda_runtime.h>
@@ -44,6 +46,8 @@ struct ExpandParams {
     unsigned long long timeout_ns;
     ExpandWorkspace ws;
     DevStatus* st;
+    unsigned long long* trace;
+    int32_t trace_cap;
 };
 
 struct SsspOp {
@@ -54,11 +58,11 @@ struct SsspOp {
         v = a.x;
         cand = du + a.y;
     }
-    __device__ __forceinline__ static bool relax(const ExpandParams& P, int v, int cand) {
-        // Read-before-atomic filter (sssp_kernel.cu:55): labels only decrease, so a stale read can
-        // only cause an extra atomic, never a missed improvement.
-        if (cand < __ldcg(P.label + v)) return cand < atomicMin(P.label + v, cand);
-        return false;
+    // Read-before-atomic filter (sssp_kernel.cu:55): labels only decrease, so a stale read can only
+    // cause an extra atomic, never a missed improvement.
+    __device__ __forceinline__ static bool want(int cand, int cur) { return cand < cur; }
+    __device__ __forceinline__ static bool commit(const ExpandParams& P, int v, int cand) {
+        return cand < atomicMin(P.label + v, cand);
     }
 };
 
@@ -69,10 +73,9 @@ struct BfsOp {
         v = __ldg(P.col + e);
         cand = du + 1;
     }
-    __device__ __forceinline__ static bool relax(const ExpandParams& P, int v, int cand) {
-        if (__ldcg(P.label + v) == DPG_UNDEFINED_LEVEL)
-            return atomicCAS(P.label + v, DPG_UNDEFINED_LEVEL, cand) == DPG_UNDEFINED_LEVEL;
-        return false;
+    __device__ __forceinline__ static bool want(int, int cur) { return cur == DPG_UNDEFINED_LEVEL; }
+    __device__ __forceinline__ static bool commit(const ExpandParams& P, int v, int cand) {
+        return atomicCAS(P.label + v, DPG_UNDEFINED_LEVEL, cand) == DPG_UNDEFINED_LEVEL;
     }
 };
 
@@ -82,68 +85,138 @@ struct PushCtx {
     int2* qse;
     uint32_t* qcount;
     uint32_t* bmp;
-    int32_t* hv;
-    int2* hse;
-    int32_t* hcpos;
-    int32_t* howner;
-    unsigned long long* hcount;
+    int4* chunks;
+    uint32_t* ccount;
 };
 
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) {
     return *reinterpret_cast<const volatile unsigned*>(p);
 }
-__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* p) {
-    return *reinterpret_cast<const volatile unsigned long long*>(p);
-}
-
-__device__ __forceinline__ void push_hub(const ExpandParams& P, const PushCtx& Q, int v, int s, int e) {
-    const unsigned nch = static_cast<unsigned>((e - s + kHubChunk - 1) / kHubChunk);
-    const unsigned long long old = atomicAdd(Q.hcount, (1ull << 32) | nch);
-    const unsigned idx = static_cast<unsigned>(old >> 32);
-    const unsigned cpos = static_cast<unsigned>(old & 0xFFFFFFFFull);
-    if (idx < P.ws.cap_hub && static_cast<unsigned long long>(cpos) + nch <= static_cast<unsigned long long>(P.ws.cap_chunks)) {
-        __stcg(Q.hv + idx, v);
-        __stcg(Q.hse + idx, make_int2(s, e));
-        __stcg(Q.hcpos + idx, static_cast<int>(cpos));
-        for (unsigned c = 0; c < nch; ++c) __stcg(Q.howner + cpos + c, static_cast<int>(idx));
-    } else {
-        raise_error(P.st, DPG_ERR_CAPACITY, 10);
+// Called by all 32 lanes together with U candidate slots each; ok[u] marks slots whose relaxation
+// improved vertex v[u]. Vertices below the chunking degree go to the small queue with one
+// warp-aggregated append for all U slots; chunked vertices get their chunk range from one
+// warp-aggregated atomic per slot and the warp writes every chunk descriptor.
+template <class Op, bool kClassify, int U>
+__device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx& Q, bool (&ok)[U],
+                                           const int (&v)[U]) {
+    bool any = false;
+#pragma unroll
+    for (int u = 0; u < U; ++u) any |= ok[u];
+    if (!__any_sync(kFullMask, any)) return;
+    if (Op::kDedup) {
+        unsigned old[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) old[u] = ok[u] ? atomicOr(Q.bmp + (v[u] >> 5), 1u << (v[u] & 31)) : 0u;
+#pragma unroll
+        for (int u = 0; u < U; ++u) ok[u] = ok[u] && (old[u] & (1u << (v[u] & 31))) == 0u;
     }
-}
-
-// Called by all 32 lanes together. `ok` marks lanes whose relaxation improved vertex v.
-template <class Op, bool kClassify>
-__device__ __forceinline__ void push_converged(const ExpandParams& P, const PushCtx& Q, bool ok, int v) {
-    if (Op::kDedup && ok) {
-        const uint32_t bit = 1u << (v & 31);
-        ok = (atomicOr(Q.bmp + (v >> 5), bit) & bit) == 0u;
+    int s[U], e[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        s[u] = 0;
+        e[u] = 0;
+        if (ok[u]) {
+            s[u] = __ldg(P.off + v[u]);
+            e[u] = __ldg(P.off + v[u] + 1);
+        }
     }
-    int s = 0, e = 0;
-    if (ok) {
-        s = __ldg(P.off + v);
-        e = __ldg(P.off + v + 1);
-        ok = e > s;  // vertices without out-edges never need expanding
+    const int lane = lane_id();
+    const unsigned lt = (1u << lane) - 1u;
+    bool chunked[U];
+    unsigned m[U];
+    unsigned cnt = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        ok[u] = ok[u] && e[u] > s[u];  // vertices without out-arcs never need expanding
+        chunked[u] = kClassify && ok[u] && (e[u] - s[u]) >= P.hub_threshold;
+        m[u] = __ballot_sync(kFullMask, ok[u] && !chunked[u]);
+        cnt += static_cast<unsigned>(__popc(m[u]));
     }
-    const bool hub = kClassify && ok && (e - s) >= P.hub_threshold;
-    const bool normal = ok && !hub;
-    const unsigned m = __ballot_sync(kFullMask, normal);
-    if (m) {
-        const int lane = lane_id();
-        const int leader = __ffs(m) - 1;
+    if (cnt) {
         unsigned base = 0;
-        if (lane == leader) base = atomicAdd(Q.qcount, static_cast<unsigned>(__popc(m)));
-        base = __shfl_sync(kFullMask, base, leader);
-        if (normal) {
-            const unsigned pos = base + static_cast<unsigned>(__popc(m & ((1u << lane) - 1u)));
-            if (pos < static_cast<unsigned long long>(P.ws.cap_v)) {
-                __stcg(Q.qv + pos, v);
-                __stcg(Q.qse + pos, make_int2(s, e));
-            } else {
-                raise_error(P.st, DPG_ERR_CAPACITY, 11);
+        if (lane == 0) base = atomicAdd(Q.qcount, cnt);
+        base = __shfl_sync(kFullMask, base, 0);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (ok[u] && !chunked[u]) {
+                const unsigned pos = base + static_cast<unsigned>(__popc(m[u] & lt));
+                if (pos < static_cast<unsigned long long>(P.ws.cap_v)) {
+                    __stcg(Q.qv + pos, v[u]);
+                    __stcg(Q.qse + pos, make_int2(s[u], e[u]));
+                } else {
+                    raise_error(P.st, DPG_ERR_CAPACITY, 11);
+                }
+            }
+            base += static_cast<unsigned>(__popc(m[u]));
+        }
+    }
+    if (kClassify) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            unsigned hm = __ballot_sync(kFullMask, chunked[u]);
+            if (!hm) continue;
+            const int nch = chunked[u] ? (e[u] - s[u] + kHubChunk - 1) / kHubChunk : 0;
+            const int incl = warp_inclusive_scan(nch);
+            const int total = __shfl_sync(kFullMask, incl, 31);
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(Q.ccount, static_cast<unsigned>(total));
+            base = __shfl_sync(kFullMask, base, 0);
+            const unsigned my_first = base + static_cast<unsigned>(incl - nch);
+            if (static_cast<unsigned long long>(base) + total > static_cast<unsigned long long>(P.ws.cap_chunks)) {
+                if (lane == 0) raise_error(P.st, DPG_ERR_CAPACITY, 10);
+                hm = 0u;
+            }
+            while (hm) {  // the whole warp writes one chunked vertex's descriptors at a time
+                const int src = __ffs(hm) - 1;
+                hm &= hm - 1u;
+                const int hv = __shfl_sync(kFullMask, v[u], src);
+                const int hs = __shfl_sync(kFullMask, s[u], src);
+                const int he = __shfl_sync(kFullMask, e[u], src);
+                const unsigned first = __shfl_sync(kFullMask, my_first, src);
+                const int hn = (he - hs + kHubChunk - 1) / kHubChunk;
+                for (int c = lane; c < hn; c += 32) {
+                    const int k0 = hs + c * kHubChunk;
+                    __stcg(Q.chunks + first + c, make_int4(hv, k0, min(he, k0 + kHubChunk), c == 0 ? 1 : 0));
+                }
             }
         }
     }
-    if (kClassify && hub) push_hub(P, Q, v, s, e);
+}
+
+// U independent relaxations per lane, issued phase by phase (U adjacency loads, U label loads, U
+// atomics, one batched push) so each warp keeps U memory operations in flight instead of one.
+template <class Op, bool kClassify, int U>
+__device__ __forceinline__ void relax_batch(const ExpandParams& P, const PushCtx& Q, const bool (&act)[U],
+                                            const int (&e)[U], const int (&du)[U]) {
+    int v[U], cand[U], cur[U];
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        v[u] = 0;
+        cand[u] = 0;
+        if (act[u]) Op::load_edge(P, e[u], du[u], v[u], cand[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) cur[u] = act[u] ? __ldcg(P.label + v[u]) : 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) ok[u] = act[u] && Op::want(cand[u], cur[u]) && Op::commit(P, v[u], cand[u]);
+    push_batch<Op, kClassify, U>(P, Q, ok, v);
+}
+
+template <class Op, bool kClassify>
+__device__ __forceinline__ void push_converged(const ExpandParams& P, const PushCtx& Q, bool ok, int v) {
+    bool okb[1] = {ok};
+    const int vb[1] = {v};
+    push_batch<Op, kClassify, 1>(P, Q, okb, vb);
+}
+
+// Relaxation of one candidate per lane (all lanes call it together).
+template <class Op, bool kClassify>
+__device__ __forceinline__ void relax_one(const ExpandParams& P, const PushCtx& Q, bool act, int e, int du) {
+    const bool a[1] = {act};
+    const int ee[1] = {e};
+    const int dd[1] = {du};
+    relax_batch<Op, kClassify, 1>(P, Q, a, ee, dd);
 }
 
 // Thread-per-vertex neighbour loops (the reference's serial loop), made warp-uniform so pushes can
@@ -153,16 +226,7 @@ __device__ __forceinline__ void serial_rows(const ExpandParams& P, const PushCtx
                                             int d, int du) {
     const int dd = act ? d : 0;
     const int wmax = __reduce_max_sync(kFullMask, dd);
-    for (int t = 0; t < wmax; ++t) {
-        bool ok = false;
-        int v = 0;
-        if (t < dd) {
-            int cand;
-            Op::load_edge(P, s + t, du, v, cand);
-            ok = Op::relax(P, v, cand);
-        }
-        push_converged<Op, kClassify>(P, Q, ok, v);
-    }
+    for (int t = 0; t < wmax; ++t) relax_one<Op, kClassify>(P, Q, t < dd, s + t, du);
 }
 
 // Scan-based gather: the warp concatenates the rows of the active lanes and relaxes 32 consecutive
@@ -180,20 +244,26 @@ __device__ __forceinline__ void warp_gather(const ExpandParams& P, const PushCtx
     ss[lane] = s;
     sdu[lane] = du;
     __syncwarp();
-    for (int base = 0; base < total; base += 32) {
-        const int k = base + lane;
-        bool ok = false;
-        int v = 0;
-        if (k < total) {
-            int r = 0;
+    constexpr int U = 4;
+    for (int base = 0; base < total; base += 32 * U) {
+        bool act[U];
+        int ee[U], dd2[U];
 #pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-                if (sx[r + step] <= k) r += step;
-            int cand;
-            Op::load_edge(P, ss[r] + (k - sx[r]), sdu[r], v, cand);
-            ok = Op::relax(P, v, cand);
+        for (int u = 0; u < U; ++u) {
+            const int k = base + 32 * u + lane;
+            act[u] = k < total;
+            ee[u] = 0;
+            dd2[u] = 0;
+            if (act[u]) {
+                int r = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (sx[r + step] <= k) r += step;
+                ee[u] = ss[r] + (k - sx[r]);
+                dd2[u] = sdu[r];
+            }
         }
-        push_converged<Op, kClassify>(P, Q, ok, v);
+        relax_batch<Op, kClassify, U>(P, Q, act, ee, dd2);
     }
     __syncwarp();
 }
@@ -202,16 +272,18 @@ __device__ __forceinline__ void warp_gather(const ExpandParams& P, const PushCtx
 template <class Op, bool kClassify>
 __device__ __forceinline__ void warp_row(const ExpandParams& P, const PushCtx& Q, int s, int d, int du) {
     const int lane = lane_id();
-    for (int base = 0; base < d; base += 32) {
-        const int t = base + lane;
-        bool ok = false;
-        int v = 0;
-        if (t < d) {
-            int cand;
-            Op::load_edge(P, s + t, du, v, cand);
-            ok = Op::relax(P, v, cand);
+    constexpr int U = 4;
+    for (int base = 0; base < d; base += 32 * U) {
+        bool act[U];
+        int ee[U], dd[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int t = base + 32 * u + lane;
+            act[u] = t < d;
+            ee[u] = s + t;
+            dd[u] = du;
         }
-        push_converged<Op, kClassify>(P, Q, ok, v);
+        relax_batch<Op, kClassify, U>(P, Q, act, ee, dd);
     }
 }
 
@@ -244,31 +316,30 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
         // Counters can pass the capacities only after a push has already raised DPG_ERR_CAPACITY
         // (which stops the loop at the barrier); the clamps keep every read inside its buffer anyway.
         const unsigned n = min(ld_volatile(P.ws.qcount + (j % 3)), static_cast<unsigned>(P.ws.cap_v));
-        const unsigned long long hc = ld_volatile(P.ws.hcount + (j % 3));
-        const unsigned nh = min(static_cast<unsigned>(hc >> 32), static_cast<unsigned>(P.ws.cap_hub));
-        const unsigned nch = min(static_cast<unsigned>(hc & 0xFFFFFFFFull), static_cast<unsigned>(P.ws.cap_chunks));
-        if (n == 0 && nh == 0) break;
+        const unsigned nch = min(ld_volatile(P.ws.ccount + (j % 3)), static_cast<unsigned>(P.ws.cap_chunks));
+        if (n == 0 && nch == 0) break;
         if (j >= P.max_iter) {
             if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(P.st, DPG_ERR_CAPACITY, 2);
             break;
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             P.ws.qcount[(j + 2) % 3] = 0u;
-            P.ws.hcount[(j + 2) % 3] = 0ull;
+            P.ws.ccount[(j + 2) % 3] = 0u;
+            if (P.trace && j < P.trace_cap) {
+                P.trace[4 * j + 0] = global_timer_ns();
+                P.trace[4 * j + 1] = n;
+                P.trace[4 * j + 2] = nch;
+                P.trace[4 * j + 3] = 0ull;
+            }
         }
         // Parity selects are written as ternaries so the pointer pairs stay in registers.
         const PushCtx Q = {p ? P.ws.qv[0] : P.ws.qv[1], p ? P.ws.qse[0] : P.ws.qse[1],
                            P.ws.qcount + (j + 1) % 3, p ? P.ws.bmp[0] : P.ws.bmp[1],
-                           p ? P.ws.hv[0] : P.ws.hv[1], p ? P.ws.hse[0] : P.ws.hse[1],
-                           p ? P.ws.hcpos[0] : P.ws.hcpos[1], p ? P.ws.howner[0] : P.ws.howner[1],
-                           P.ws.hcount + (j + 1) % 3};
+                           p ? P.ws.chunks[0] : P.ws.chunks[1], P.ws.ccount + (j + 1) % 3};
         const int32_t* qv_cur = p ? P.ws.qv[1] : P.ws.qv[0];
         const int2* qse_cur = p ? P.ws.qse[1] : P.ws.qse[0];
         uint32_t* bmp_cur = p ? P.ws.bmp[1] : P.ws.bmp[0];
-        const int32_t* hv_cur = p ? P.ws.hv[1] : P.ws.hv[0];
-        const int2* hse_cur = p ? P.ws.hse[1] : P.ws.hse[0];
-        const int32_t* hcpos_cur = p ? P.ws.hcpos[1] : P.ws.hcpos[0];
-        const int32_t* howner_cur = p ? P.ws.howner[1] : P.ws.howner[0];
+        const int4* chunks_cur = p ? P.ws.chunks[1] : P.ws.chunks[0];
         const unsigned fchunks = (n + 31u) / 32u;
 
         if (POL == DPG_SOL_BLOCK) {
@@ -317,18 +388,16 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                     const int total = c_total;
                     for (int base = 0; base < total; base += kBlock) {
                         const int k = base + static_cast<int>(threadIdx.x);
-                        bool ok = false;
-                        int v = 0;
+                        int ee = 0, dd = 0;
                         if (k < total) {
                             int rr = 0;
 #pragma unroll
                             for (int step = kBlock / 2; step > 0; step >>= 1)
                                 if (rr + step < kBlock && c_excl[rr + step] <= k) rr += step;
-                            int cand;
-                            Op::load_edge(P, c_start[rr] + (k - c_excl[rr]), c_du[rr], v, cand);
-                            ok = Op::relax(P, v, cand);
+                            ee = c_start[rr] + (k - c_excl[rr]);
+                            dd = c_du[rr];
                         }
-                        push_converged<Op, false>(P, Q, ok, v);
+                        relax_one<Op, false>(P, Q, k < total, ee, dd);
                     }
                     __syncthreads();
                     if (threadIdx.x == 0) c_n = 0;
@@ -340,34 +409,26 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
             const unsigned total_items = hub_items + fchunks;
             for (unsigned item = gwarp; item < total_items; item += nwarps) {
                 if (kClassify && item < hub_items) {
-                    // Grid-wide consolidation: one 256-edge chunk of a hub row.
-                    const int c = static_cast<int>(item);
-                    const int h = __ldcg(howner_cur + c);
-                    if (static_cast<unsigned>(h) >= nh) {  // warp-uniform: every lane read the same c
-                        if (lane == 0) raise_error(P.st, DPG_ERR_CAPACITY, 12);
-                        continue;
-                    }
-                    const int v0 = __ldcg(hv_cur + h);
-                    const int2 se = __ldcg(hse_cur + h);
-                    const int cp = __ldcg(hcpos_cur + h);
+                    // Grid-wide consolidation: one chunk (<= 256 arcs) of a chunked vertex.
+                    const int4 C = __ldcg(chunks_cur + item);
+                    const int v0 = C.x, k0 = C.y, k1 = C.z;
                     const int du = __ldcg(P.label + v0);
-                    const int k0 = se.x + (c - cp) * kHubChunk;
-                    const int k1 = min(se.y, k0 + kHubChunk);
-                    if (c == cp && lane == 0) {
+                    if (C.w && lane == 0) {
                         if (Op::kDedup) __stcg(bmp_cur + (v0 >> 5), 0u);
                         my_pops += 1;
                     }
                     if (lane == 0) my_edges += static_cast<unsigned long long>(k1 - k0);
-                    for (int base = k0; base < k1; base += 32) {
-                        const int e = base + lane;
-                        bool ok = false;
-                        int v = 0;
-                        if (e < k1) {
-                            int cand;
-                            Op::load_edge(P, e, du, v, cand);
-                            ok = Op::relax(P, v, cand);
+                    {
+                        constexpr int U = kHubChunk / 32;  // the whole chunk in one batch
+                        bool act[U];
+                        int ee[U], dd[U];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            ee[u] = k0 + 32 * u + lane;
+                            act[u] = ee[u] < k1;
+                            dd[u] = du;
                         }
-                        push_converged<Op, kClassify>(P, Q, ok, v);
+                        relax_batch<Op, kClassify, U>(P, Q, act, ee, dd);
                     }
                     continue;
                 }
@@ -417,7 +478,15 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
         if (my_edges) atomicAdd(&P.st->edges, my_edges);
         if (my_pops) atomicAdd(&P.st->pops, my_pops);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) P.st->iterations = static_cast<unsigned long long>(j);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        P.st->iterations = static_cast<unsigned long long>(j);
+        if (P.trace && j < P.trace_cap) {  // end marker: time the last barrier was passed
+            P.trace[4 * j + 0] = global_timer_ns();
+            P.trace[4 * j + 1] = 0ull;
+            P.trace[4 * j + 2] = 0ull;
+            P.trace[4 * j + 3] = 1ull;
+        }
+    }
 }
 
 __global__ void expand_init_kernel(ExpandParams P, int32_t source, int32_t init_label, int classify) {
@@ -428,30 +497,30 @@ __global__ void expand_init_kernel(ExpandParams P, int32_t source, int32_t init_
         P.ws.bmp[0][w] = 0u;
         P.ws.bmp[1][w] = 0u;
     }
+    // The source enters the first frontier: chunked when its degree calls for it.
+    const int s = P.off[source];
+    const int e = P.off[source + 1];
+    const bool chunked = classify && e > s && e - s >= P.hub_threshold;
+    const int nch = chunked ? (e - s + kHubChunk - 1) / kHubChunk : 0;
+    for (int64_t c = tid; c < nch; c += stride) {
+        const int k0 = s + static_cast<int>(c) * kHubChunk;
+        P.ws.chunks[0][c] = make_int4(source, k0, min(e, k0 + kHubChunk), c == 0 ? 1 : 0);
+    }
     if (tid == 0) {
         for (int k = 0; k < 3; ++k) {
             P.ws.qcount[k] = 0u;
-            P.ws.hcount[k] = 0ull;
+            P.ws.ccount[k] = 0u;
         }
         P.st->bar_count = 0u;
         P.st->iterations = 0ull;
         P.st->edges = 0ull;
         P.st->pops = 0ull;
-        const int s = P.off[source];
-        const int e = P.off[source + 1];
-        if (e > s) {
-            if (classify && e - s >= P.hub_threshold) {
-                const int nch = (e - s + kHubChunk - 1) / kHubChunk;
-                P.ws.hv[0][0] = source;
-                P.ws.hse[0][0] = make_int2(s, e);
-                P.ws.hcpos[0][0] = 0;
-                for (int c = 0; c < nch; ++c) P.ws.howner[0][c] = 0;
-                P.ws.hcount[0] = (1ull << 32) | static_cast<unsigned long long>(nch);
-            } else {
-                P.ws.qv[0][0] = source;
-                P.ws.qse[0][0] = make_int2(s, e);
-                P.ws.qcount[0] = 1u;
-            }
+        if (chunked) {
+            P.ws.ccount[0] = static_cast<unsigned>(nch);
+        } else if (e > s) {
+            P.ws.qv[0][0] = source;
+            P.ws.qse[0][0] = make_int2(s, e);
+            P.ws.qcount[0] = 1u;
         }
     }
 }
@@ -478,13 +547,11 @@ const void* pick_kernel(int solution) {
 
 }  // namespace
 
-void expand_workspace_caps(int32_t V, int64_t E, int32_t min_hub_degree, int64_t* cap_hub,
-                           int64_t* cap_chunks) {
-    const int64_t d = min_hub_degree < 1 ? 1 : min_hub_degree;
-    int64_t hubs = E / d + 1;
-    if (hubs > static_cast<int64_t>(V) + 1) hubs = static_cast<int64_t>(V) + 1;
-    *cap_hub = hubs;
-    *cap_chunks = E / kHubChunk + hubs + 1;
+int64_t expand_chunk_capacity(int32_t V, int64_t E, int32_t min_chunked_degree) {
+    const int64_t d = min_chunked_degree < 1 ? 1 : min_chunked_degree;
+    int64_t vertices = E / d + 1;
+    if (vertices > static_cast<int64_t>(V) + 1) vertices = static_cast<int64_t>(V) + 1;
+    return E / kHubChunk + vertices + 1;
 }
 
 cudaError_t launch_expand(const ExpandLaunch& L, const ExpandWorkspace& ws, DevStatus* st,
@@ -509,6 +576,8 @@ cudaError_t launch_expand(const ExpandLaunch& L, const ExpandWorkspace& ws, DevS
     P.timeout_ns = L.timeout_ns;
     P.ws = ws;
     P.st = st;
+    P.trace = L.trace;
+    P.trace_cap = L.trace_cap;
     const int classify = (L.solution == DPG_SOL_GRID || L.solution == DPG_SOL_BINNED) ? 1 : 0;
     const int32_t init_label = L.bfs ? DPG_UNDEFINED_LEVEL : DPG_INF_COST;
     int init_blocks = static_cast<int>((static_cast<int64_t>(L.V) + kBlock - 1) / kBlock);

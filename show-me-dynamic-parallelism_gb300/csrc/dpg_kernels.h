@@ -32,23 +32,19 @@ struct HookScope {
 
 // ---- frontier expansion (SSSP / BFS) ------------------------------------------------------------
 
-// Edges per grid-wide hub chunk: hubs are split into chunks of this many adjacency entries and the
-// chunks are spread over every warp of the persistent grid.
+// Arcs per grid-wide chunk: every vertex at or above the chunking degree is cut into chunks of this
+// many adjacency entries at push time, and the chunks are spread over every warp of the grid.
 constexpr int kHubChunk = 256;
 
 // Device buffers of one expansion. Index [p] is the frontier parity (iteration & 1).
 struct ExpandWorkspace {
-    int32_t* qv[2];        // frontier vertex ids
-    int2* qse[2];          // frontier (row start, row end) so the pop needs no offsets lookup
+    int32_t* qv[2];        // small-degree frontier: vertex ids
+    int2* qse[2];          // small-degree frontier: (row start, row end), so a pop needs no offsets lookup
     uint32_t* bmp[2];      // "already queued this iteration" bit per vertex (SSSP)
-    int32_t* hv[2];        // hub vertices (degree >= hub threshold), grid-wide consolidation buffer
-    int2* hse[2];          // hub (row start, row end)
-    int32_t* hcpos[2];     // first chunk index of each hub in the iteration's chunk space
-    int32_t* howner[2];    // chunk -> hub index
-    uint32_t* qcount;      // [3] frontier lengths, rotated so resets never race with pushes
-    unsigned long long* hcount;  // [3] packed (hub count << 32 | chunk count)
+    int4* chunks[2];       // chunked frontier: {vertex, arc begin, arc end, 1 on a vertex's first chunk}
+    uint32_t* qcount;      // [3] small-frontier lengths, rotated so resets never race with pushes
+    uint32_t* ccount;      // [3] chunk counts, rotated the same way
     int64_t cap_v;
-    int64_t cap_hub;
     int64_t cap_chunks;
     int32_t bmp_words;
 };
@@ -67,12 +63,13 @@ struct ExpandLaunch {
     int32_t hub_threshold;
     int32_t max_iter;
     unsigned long long timeout_ns;
+    unsigned long long* trace = nullptr;  // nullable: [trace_cap][4] {t_ns, small frontier, chunks, 0}
+    int32_t trace_cap = 0;
 };
 
-// Bytes of every workspace buffer for a graph of V vertices and E arcs with the given minimum hub
-// degree; used to size the context arena.
-void expand_workspace_caps(int32_t V, int64_t E, int32_t min_hub_degree, int64_t* cap_hub,
-                           int64_t* cap_chunks);
+// Chunk capacity per parity for a graph of V vertices and E arcs when vertices of degree >=
+// min_chunked_degree are chunked: sum of ceil(deg/256) over distinct vertices of one iteration.
+int64_t expand_chunk_capacity(int32_t V, int64_t E, int32_t min_chunked_degree);
 
 cudaError_t launch_expand(const ExpandLaunch& L, const ExpandWorkspace& ws, DevStatus* st,
                           cudaStream_t stream, int sm_count, int* grid_out, int* block_out,
@@ -116,11 +113,13 @@ struct RowGatherLaunch {
     const int32_t* col;
     const float* vals;      // SpMV values; nullptr for PageRank
     const float* x;         // SpMV x / PageRank contribution in
+    int32_t hot;            // x[0, hot) is staged in shared memory (the most gathered renamed columns)
     float* y;               // SpMV y / PageRank contribution out
     float* partial;         // [plan.nseg] hub-segment partial sums
     int32_t V;
     // PageRank only
     const int32_t* outdeg;
+    const int32_t* perm;    // nullable: contribution of row v goes to y[perm[v]] (renamed columns)
     float* rank_out;        // nullable: written when this sweep's ranks are needed
     const float* rank_prev; // nullable: convergence check against it
     float damping;
@@ -134,8 +133,19 @@ struct RowGatherLaunch {
     unsigned* nonstop;      // nullable: set to 1 when some |new-old| > epsilon
 };
 
+// Column renaming by frequency (dpg_layout.cu).
+cudaError_t launch_column_histogram(const int32_t* col, int64_t E, int32_t* counts, cudaStream_t s, int sm_count);
+cudaError_t launch_relabel_columns(const int32_t* col, const int32_t* perm, int64_t E, int32_t* out, cudaStream_t s,
+                                   int sm_count);
+cudaError_t launch_gather_by_index(const float* x, const int32_t* inv, int32_t V, float* out, cudaStream_t s,
+                                   int sm_count);
+// perm[old] = new, inv[new] = old; most frequent columns first (by bit length of the count), ties by id.
+void frequency_order(const int32_t* counts, int32_t V, int32_t* perm, int32_t* inv);
+
 // Grid shape used by the row-gather kernels (needed to size dpart/dfix).
 void rowgather_grid(int sm_count, int* gather_blocks, int* fix_blocks, int* block_threads);
+// Shared memory the gather kernel needs besides the hot-value cache.
+size_t rowgather_staging_bytes();
 
 cudaError_t launch_spmv(const RowGatherLaunch& L, DevStatus* st, cudaStream_t stream, int sm_count,
                         LaunchHook* hook);

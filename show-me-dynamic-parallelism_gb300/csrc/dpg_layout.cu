@@ -1,0 +1,82 @@
+// Gather-locality layout for the row gathers: column ids renamed by descending column frequency.
+//
+// In a pull PageRank sweep or an SpMV, every nonzero gathers one 4-byte value at its column id. On
+// R-MAT graphs the columns are extremely skewed (at scale 22 the 16 K most frequent columns take 42 %
+// of all gathers; half the vertices never appear as a column), but the input ids scatter those hot
+// values over the whole vector, so every gather moves its own 32-byte L2 sector. Renaming columns
+// so the most frequent come first packs the hot values into a few KB that stay in L1 and share
+// sectors. Only column ids change: rows, and the order of nonzeros inside each row, are untouched,
+// so every sum is taken in the same order and results are bit-identical with or without the
+// renaming.
+//
+// The order is "by frequency class, then by id": class = bit length of the column count, so the
+// stable multi-split below needs 33 buckets instead of a full sort.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "dpg_kernels.h"
+
+namespace dpg {
+namespace {
+
+__global__ void column_histogram_kernel(const int32_t* __restrict__ col, int64_t E, int32_t* counts) {
+    for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < E;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        atomicAdd(counts + __ldg(col + e), 1);
+}
+
+__global__ void relabel_columns_kernel(const int32_t* __restrict__ col, const int32_t* __restrict__ perm, int64_t E,
+                                       int32_t* __restrict__ out) {
+    for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < E;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[e] = __ldg(perm + __ldg(col + e));
+}
+
+__global__ void gather_by_index_kernel(const float* __restrict__ x, const int32_t* __restrict__ inv, int32_t V,
+                                       float* __restrict__ out) {
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < V;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = __ldg(x + __ldg(inv + i));
+}
+
+}  // namespace
+
+cudaError_t launch_column_histogram(const int32_t* col, int64_t E, int32_t* counts, cudaStream_t s, int sm_count) {
+    if (E > 0) column_histogram_kernel<<<sm_count * 8, 256, 0, s>>>(col, E, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_relabel_columns(const int32_t* col, const int32_t* perm, int64_t E, int32_t* out, cudaStream_t s,
+                                   int sm_count) {
+    if (E > 0) relabel_columns_kernel<<<sm_count * 8, 256, 0, s>>>(col, perm, E, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_by_index(const float* x, const int32_t* inv, int32_t V, float* out, cudaStream_t s,
+                                   int sm_count) {
+    if (V > 0) gather_by_index_kernel<<<sm_count * 4, 256, 0, s>>>(x, inv, V, out);
+    return cudaGetLastError();
+}
+
+void frequency_order(const int32_t* counts, int32_t V, int32_t* perm, int32_t* inv) {
+    // Stable multi-split on the bit length of the count, largest class first.
+    int64_t bucket[34] = {0};
+    auto cls = [](int32_t c) { return c <= 0 ? 0 : 32 - __builtin_clz(static_cast<unsigned>(c)); };
+    for (int32_t v = 0; v < V; ++v) ++bucket[cls(counts[v])];
+    int64_t start[34];
+    int64_t acc = 0;
+    for (int b = 33; b >= 0; --b) {
+        start[b] = acc;
+        acc += bucket[b];
+    }
+    for (int32_t v = 0; v < V; ++v) {
+        const int32_t n = static_cast<int32_t>(start[cls(counts[v])]++);
+        perm[v] = n;
+        inv[n] = v;
+    }
+}
+
+}  // namespace dpg

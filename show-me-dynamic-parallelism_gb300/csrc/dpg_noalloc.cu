@@ -6,7 +6,7 @@
 // forbid cudaMalloc/cudaFree behind their back. The regular entry points need a dpg_ctx and a
 // dpg_graph, and both allocate (status block, stream, frontier arena, device CSR). This one runs
 // the same persistent SSSP kernel (binned work mapping) on caller-owned inputs and outputs, with
-// its frontier queues, bitmaps, hub buffers and status word carved out of one file-scope
+// its frontier queues, bitmaps, chunk lists and status word carved out of one file-scope
 // __device__ array.
 //
 // Limits and sharing rules:
@@ -41,27 +41,24 @@ constexpr int kMaxDevices = 64;
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct NoAllocLayout {
-    size_t qv, qse, bmp, hv, hse, hcpos, howner, qcount, hcount, status, total;
+    size_t qv, qse, bmp, chunks, qcount, ccount, status, total;
 };
 
 constexpr NoAllocLayout layout_for(int64_t V, int64_t E) {
     NoAllocLayout L{};
     const int64_t cap_v = V + 1;
-    const int64_t hubs_raw = E / kNoAllocHubDegree + 1;
-    const int64_t cap_hub = hubs_raw < V + 1 ? hubs_raw : V + 1;
-    const int64_t cap_chunks = E / kHubChunk + cap_hub + 1;
+    const int64_t chunked_raw = E / kNoAllocHubDegree + 1;
+    const int64_t chunked = chunked_raw < V + 1 ? chunked_raw : V + 1;
+    const int64_t cap_chunks = E / kHubChunk + chunked + 1;
     const int64_t words = (V + 31) / 32 + 1;
     L.qv = align256(sizeof(int32_t) * size_t(cap_v));
     L.qse = align256(sizeof(int2) * size_t(cap_v));
     L.bmp = align256(sizeof(uint32_t) * size_t(words));
-    L.hv = align256(sizeof(int32_t) * size_t(cap_hub));
-    L.hse = align256(sizeof(int2) * size_t(cap_hub));
-    L.hcpos = align256(sizeof(int32_t) * size_t(cap_hub));
-    L.howner = align256(sizeof(int32_t) * size_t(cap_chunks));
+    L.chunks = align256(sizeof(int4) * size_t(cap_chunks));
     L.qcount = align256(sizeof(uint32_t) * 4);
-    L.hcount = align256(sizeof(unsigned long long) * 4);
+    L.ccount = align256(sizeof(uint32_t) * 4);
     L.status = align256(sizeof(DevStatus));
-    L.total = 2 * (L.qv + L.qse + L.bmp + L.hv + L.hse + L.hcpos + L.howner) + L.qcount + L.hcount + L.status;
+    L.total = 2 * (L.qv + L.qse + L.bmp + L.chunks) + L.qcount + L.ccount + L.status;
     return L;
 }
 
@@ -120,20 +117,17 @@ extern "C" dpg_status dpg_sssp_noalloc_dev(int32_t V, int64_t E, const int32_t* 
     ExpandWorkspace ws;
     memset(&ws, 0, sizeof(ws));
     ws.cap_v = int64_t(V) + 1;
-    expand_workspace_caps(V, E, kNoAllocHubDegree, &ws.cap_hub, &ws.cap_chunks);
+    ws.cap_chunks = expand_chunk_capacity(V, E, kNoAllocHubDegree);
     ws.bmp_words = (V + 31) / 32 + 1;
     unsigned char* p = base;
     for (int k = 0; k < 2; ++k) {
         ws.qv[k] = reinterpret_cast<int32_t*>(p); p += Lo.qv;
         ws.qse[k] = reinterpret_cast<int2*>(p); p += Lo.qse;
         ws.bmp[k] = reinterpret_cast<uint32_t*>(p); p += Lo.bmp;
-        ws.hv[k] = reinterpret_cast<int32_t*>(p); p += Lo.hv;
-        ws.hse[k] = reinterpret_cast<int2*>(p); p += Lo.hse;
-        ws.hcpos[k] = reinterpret_cast<int32_t*>(p); p += Lo.hcpos;
-        ws.howner[k] = reinterpret_cast<int32_t*>(p); p += Lo.howner;
+        ws.chunks[k] = reinterpret_cast<int4*>(p); p += Lo.chunks;
     }
     ws.qcount = reinterpret_cast<uint32_t*>(p); p += Lo.qcount;
-    ws.hcount = reinterpret_cast<unsigned long long*>(p); p += Lo.hcount;
+    ws.ccount = reinterpret_cast<uint32_t*>(p); p += Lo.ccount;
     DevStatus* st = reinterpret_cast<DevStatus*>(p);
 
     cudaStream_t cs = static_cast<cudaStream_t>(stream);

@@ -12,6 +12,8 @@
 //   - a row of degree > 255 (a hub) is split into 256-nonzero segments whose partial sums are
 //     combined afterwards, in segment order, by the hub fix-up kernel.
 // Every sum has a fixed order, so results are bit-reproducible run to run; no float atomics.
+// With renamed columns (dpg_layout.cu) `col` holds the new ids, `x` is indexed by them, and the
+// PageRank epilogue writes row v's contribution at perm[v].
 // PageRank folds rank/outdeg into the sweep's epilogue (contrib[v] = rank[v]/outdeg[v]), so the
 // gather reads one 4-byte value per in-edge instead of the reference's rank and outdegree pair and
 // divide per edge (pagerank_kernel.cu:114), and sums the dangling mass on the device (the reference
@@ -26,8 +28,11 @@
 namespace dpg {
 namespace {
 
-constexpr int kBlock = 256;
+// One 1024-thread CTA per SM: its dynamic shared memory holds the hot-value cache (the first
+// `hot` renamed entries of x, i.e. the most gathered columns) and the 32 warps' tile staging.
+constexpr int kBlock = 1024;
 constexpr int kWarps = kBlock / 32;
+constexpr int kInitBlock = 256;
 constexpr int kIpl = kRowTileItems / 32;  // merge items per lane
 constexpr int kFixBlock = 256;
 // Shared-memory index with one pad word per 32: lane l walking items 8l.. then hits 32 distinct banks
@@ -37,11 +42,16 @@ __device__ __forceinline__ int pad(int i) { return i + (i >> 5); }
 
 enum { kModeSpmv = 0, kModePagerank = 1 };
 
+// x[c], from the shared-memory cache when c is one of the `hot` most gathered (renamed) columns.
+__device__ __forceinline__ float gather_x(const RowGatherLaunch& L, const float* s_hot, int c) {
+    return c < L.hot ? s_hot[c] : __ldg(L.x + c);
+}
+
 template <int MODE>
-__device__ __forceinline__ float load_product(const RowGatherLaunch& L, int e) {
+__device__ __forceinline__ float load_product(const RowGatherLaunch& L, const float* s_hot, int e) {
     const int c = __ldg(L.col + e);
-    if (MODE == kModeSpmv) return __ldg(L.vals + e) * __ldg(L.x + c);
-    return __ldg(L.x + c);
+    if (MODE == kModeSpmv) return __ldg(L.vals + e) * gather_x(L, s_hot, c);
+    return gather_x(L, s_hot, c);
 }
 
 // PageRank epilogue of one row: new rank, next contribution, dangling mass, convergence flag.
@@ -51,8 +61,10 @@ __device__ __forceinline__ void pr_epilogue(const RowGatherLaunch& L, int v, flo
     if (L.rank_out) L.rank_out[v] = nv;
     if (L.rank_prev && fabsf(nv - __ldg(L.rank_prev + v)) > L.epsilon) *L.nonstop = 1u;
     const int od = __ldg(L.outdeg + v);
-    L.y[v] = od > 0 ? nv / static_cast<float>(od) : 0.0f;
-    if (od == 0) dang += static_cast<double>(nv);
+    // Only vertices with out-arcs are ever gathered (they are the columns), so dangling vertices
+    // write no contribution at all.
+    if (od > 0) L.y[L.perm ? __ldg(L.perm + v) : v] = nv / static_cast<float>(od);
+    else dang += static_cast<double>(nv);
 }
 
 __device__ __forceinline__ float pr_base(const RowGatherLaunch& L) {
@@ -61,16 +73,17 @@ __device__ __forceinline__ float pr_base(const RowGatherLaunch& L) {
 
 template <int MODE>
 __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
-    __shared__ int s_re[kWarps][kPadded];
-    __shared__ float s_val[kWarps][kPadded];
-    __shared__ float s_out[kWarps][kPadded];
+    extern __shared__ __align__(16) unsigned char rg_smem[];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int gwarp = blockIdx.x * kWarps + warp;
     const int nwarps = gridDim.x * kWarps;
-    int* re = s_re[warp];
-    float* val = s_val[warp];
-    float* out = s_out[warp];
+    int* re = reinterpret_cast<int*>(rg_smem) + warp * (3 * kPadded);
+    float* val = reinterpret_cast<float*>(re + kPadded);
+    float* out = val + kPadded;
+    float* s_hot = reinterpret_cast<float*>(rg_smem) + kWarps * 3 * kPadded;
+    for (int i = threadIdx.x; i < L.hot; i += kBlock) s_hot[i] = __ldg(L.x + i);
+    __syncthreads();
     float base = 0.0f;
     if (MODE == kModePagerank) base = pr_base(L);
     double dang = 0.0;
@@ -84,7 +97,7 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
 #pragma unroll
             for (int i = 0; i < kIpl; ++i) {
                 const int j = i * 32 + lane;
-                if (j < nnz) acc += load_product<MODE>(L, nb + j);
+                if (j < nnz) acc += load_product<MODE>(L, s_hot, nb + j);
             }
             acc = warp_sum_f32(acc);
             if (lane == 0) L.partial[-(nrows + 1)] = acc;
@@ -102,7 +115,7 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
         for (int i = 0; i < kIpl; ++i) {
             const int j = i * 32 + lane;
             if (j < nnz) {
-                float pv = __ldg(L.x + cols[i]);
+                float pv = gather_x(L, s_hot, cols[i]);
                 if (MODE == kModeSpmv) pv *= __ldg(L.vals + nb + j);
                 val[pad(j)] = pv;
             }
@@ -222,16 +235,16 @@ __global__ void __launch_bounds__(kFixBlock) hub_fixup_kernel(RowGatherLaunch L,
 }
 
 // Initial contribution vector and its dangling mass. Uses the gather grid so dpart lines up.
-__global__ void __launch_bounds__(kBlock) pr_init_kernel(RowGatherLaunch L, float init_rank, float* rank_prev) {
+__global__ void __launch_bounds__(kInitBlock) pr_init_kernel(RowGatherLaunch L, float init_rank, float* rank_prev) {
     const int lane = threadIdx.x & 31;
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nthreads = gridDim.x * blockDim.x;
     double dang = 0.0;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < L.V; v += nthreads) {
         const int od = __ldg(L.outdeg + v);
-        L.y[v] = od > 0 ? init_rank / static_cast<float>(od) : 0.0f;
+        if (od > 0) L.y[L.perm ? __ldg(L.perm + v) : v] = init_rank / static_cast<float>(od);
+        else dang += static_cast<double>(init_rank);
         if (rank_prev) rank_prev[v] = init_rank;
-        if (od == 0) dang += static_cast<double>(init_rank);
     }
     dang = warp_sum_f64(dang);
     if (lane == 0) L.dpart[gwarp] = dang;
@@ -240,11 +253,27 @@ __global__ void __launch_bounds__(kBlock) pr_init_kernel(RowGatherLaunch L, floa
 }  // namespace
 
 void rowgather_grid(int sm_count, int* gather_blocks, int* fix_blocks, int* block_threads) {
-    // 24.75 KB of shared memory per 256-thread CTA: up to 8 CTAs (64 warps) per SM.
-    *gather_blocks = sm_count * 8;
+    *gather_blocks = sm_count;
     *fix_blocks = sm_count * 2;
     *block_threads = kBlock;
 }
+
+size_t rowgather_staging_bytes() { return sizeof(int) * kWarps * 3 * kPadded; }
+
+namespace {
+
+// Sets the kernel's dynamic shared-memory limit to what this launch needs (once per size).
+template <int MODE>
+cudaError_t prepare_rowgather(size_t bytes) {
+    static size_t configured = 0;
+    if (bytes <= configured) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(rowgather_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(bytes));
+    if (e == cudaSuccess) configured = bytes;
+    return e;
+}
+
+}  // namespace
 
 void build_row_plan(const int32_t* off, int32_t V, RowPlanHost* plan) {
     plan->tiles.clear();
@@ -285,11 +314,14 @@ cudaError_t launch_spmv(const RowGatherLaunch& L, DevStatus* st, cudaStream_t st
                         LaunchHook* hook) {
     int gb, fb, bt;
     rowgather_grid(sm_count, &gb, &fb, &bt);
+    const size_t smem = rowgather_staging_bytes() + sizeof(float) * static_cast<size_t>(L.hot);
+    cudaError_t err = prepare_rowgather<kModeSpmv>(smem);
+    if (err != cudaSuccess) return err;
     {
         HookScope hs(hook, DPG_KERNEL_ROWGATHER, stream);
-        rowgather_kernel<kModeSpmv><<<gb, bt, 0, stream>>>(L);
+        rowgather_kernel<kModeSpmv><<<gb, bt, smem, stream>>>(L);
     }
-    cudaError_t err = cudaGetLastError();
+    err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     if (L.plan.nhub_small + L.plan.nhub_big > 0) {
         HookScope hs(hook, DPG_KERNEL_FIXUP, stream);
@@ -303,11 +335,14 @@ cudaError_t launch_pagerank_sweep(const RowGatherLaunch& L, DevStatus* st, cudaS
                                   LaunchHook* hook) {
     int gb, fb, bt;
     rowgather_grid(sm_count, &gb, &fb, &bt);
+    const size_t smem = rowgather_staging_bytes() + sizeof(float) * static_cast<size_t>(L.hot);
+    cudaError_t err = prepare_rowgather<kModePagerank>(smem);
+    if (err != cudaSuccess) return err;
     {
         HookScope hs(hook, DPG_KERNEL_ROWGATHER, stream);
-        rowgather_kernel<kModePagerank><<<gb, bt, 0, stream>>>(L);
+        rowgather_kernel<kModePagerank><<<gb, bt, smem, stream>>>(L);
     }
-    cudaError_t err = cudaGetLastError();
+    err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     {
         HookScope hs(hook, DPG_KERNEL_FIXUP, stream);
@@ -322,7 +357,8 @@ cudaError_t launch_pagerank_init(const RowGatherLaunch& L, float init_rank, floa
     rowgather_grid(sm_count, &gb, &fb, &bt);
     {
         HookScope hs(hook, DPG_KERNEL_INIT, stream);
-        pr_init_kernel<<<gb, bt, 0, stream>>>(L, init_rank, rank_prev);
+        // Same number of warps as the gather grid, so dpart[] lines up one slot per warp.
+        pr_init_kernel<<<gb * (bt / kInitBlock), kInitBlock, 0, stream>>>(L, init_rank, rank_prev);
     }
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;

@@ -171,3 +171,24 @@ def test_spmv_pagerank_rmat22_full_size(ctx, orc):
     r = dpg.pagerank(ctx, dpg.Graph(ctx, in_off, in_col), od, iterations=20)
     r64, _ = orc.pagerank_f64(in_off, in_col, od, iterations=20)
     assert np.max(np.abs(r - r64) / r64) <= TOL
+
+
+@pytest.mark.parametrize("name", ["rmat16", "hubs"])
+def test_column_renaming_is_bit_identical(ctx, graphs, name):
+    g = graphs[name]
+    rng = np.random.default_rng(9)
+    vals = rng.uniform(0, 1, g.E).astype(np.float32)
+    x = rng.uniform(-1, 1, g.V).astype(np.float32)
+    plain = dpg.Graph(ctx, g.offsets, g.col)
+    plain.set_relabel(False)
+    renamed = dpg.Graph(ctx, g.offsets, g.col)
+    a = dpg.spmv(ctx, plain, vals, x)
+    b = dpg.spmv(ctx, renamed, vals, x)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    in_off, in_col, od = _pr_inputs(g)
+    gp = dpg.Graph(ctx, in_off, in_col)
+    gp.set_relabel(False)
+    gr = dpg.Graph(ctx, in_off, in_col)
+    ra = dpg.pagerank(ctx, gp, od)
+    rb = dpg.pagerank(ctx, gr, od)
+    assert np.array_equal(ra.view(np.uint32), rb.view(np.uint32))
