@@ -136,6 +136,14 @@ dpg_status dpg_bfs(dpg_ctx* ctx, const dpg_graph* g, int32_t source, const dpg_e
 dpg_status dpg_bfs_dev(dpg_ctx* ctx, const dpg_graph* g, int32_t source,
                        const dpg_expand_opts* opts, int32_t* d_level);
 
+/* ---- graph colouring (replaces GRAPH_COLOR_GPU, apps/graph-color/src/graph_color_wrapper.cu:210-238) */
+/* color[v] = the round in which the reference's gclr_bitmap_kernel (graph_color_kernel.cu:28-49)
+ * colours v: 1 + the largest colour among out-neighbours u < v (1 when there is none). Runs as one
+ * persistent level-by-level pass over the transposed graph (built on the device on first use). Only
+ * the timeout/iteration fields of opts are used. */
+dpg_status dpg_color(dpg_ctx* ctx, const dpg_graph* g, const dpg_expand_opts* opts, int32_t* h_color);
+dpg_status dpg_color_dev(dpg_ctx* ctx, const dpg_graph* g, const dpg_expand_opts* opts, int32_t* d_color);
+
 /* ---- SpMV (replaces SpMV_GPU / csr_spmv_kernel, apps/SpMV/src/SpMV_kernel.cu:81-96) ------------ */
 /* y[r] = sum over row r of vals[e] * x[col[e]]; FP32 in and out, deterministic summation order. */
 dpg_status dpg_spmv_f32(dpg_ctx* ctx, const dpg_graph* g, const float* h_vals, const float* h_x,

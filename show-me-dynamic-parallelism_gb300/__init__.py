@@ -132,6 +132,8 @@ _SIGS = {
     "dpg_sssp_dev": [_P, _P, c_int32, POINTER(ExpandOpts), _P],
     "dpg_bfs": [_P, _P, c_int32, POINTER(ExpandOpts), _P],
     "dpg_bfs_dev": [_P, _P, c_int32, POINTER(ExpandOpts), _P],
+    "dpg_color": [_P, _P, POINTER(ExpandOpts), _P],
+    "dpg_color_dev": [_P, _P, POINTER(ExpandOpts), _P],
     "dpg_spmv_f32": [_P, _P, _P, _P, _P],
     "dpg_spmv_f32_dev": [_P, _P, _P, _P, _P],
     "dpg_pagerank_f32": [_P, _P, _P, POINTER(PrOpts), _P],
@@ -457,6 +459,19 @@ def bfs(ctx: Context, g: Graph, source: int, **opts) -> np.ndarray:
 def bfs_dev(ctx: Context, g: Graph, source: int, d_level: int, **opts) -> None:
     o = expand_opts(**opts)
     _check(lib().dpg_bfs_dev(ctx.handle, g.handle, source, byref(o), c_void_p(d_level)))
+
+
+def color(ctx: Context, g: Graph, **opts) -> np.ndarray:
+    """GRAPH_COLOR_GPU: colour of each vertex under the reference's round rule (1-based)."""
+    out = np.empty(max(g.V, 1), np.int32)
+    o = expand_opts(**opts)
+    _check(lib().dpg_color(ctx.handle, g.handle, byref(o), _ptr(out)))
+    return out[:g.V]
+
+
+def color_dev(ctx: Context, g: Graph, d_color: int, **opts) -> None:
+    o = expand_opts(**opts)
+    _check(lib().dpg_color_dev(ctx.handle, g.handle, byref(o), c_void_p(d_color)))
 
 
 def spmv(ctx: Context, g: Graph, vals, x) -> np.ndarray:

@@ -36,6 +36,7 @@ APP_SOURCES = {
     "gpu-bfs-rec": "app_bfs_rec.cpp",
     "gpu-SpMV": "app_spmv.cpp",
     "gpu-pg": "app_pagerank.cpp",
+    "gpu-graph-color": "app_graph_color.cpp",
 }
 
 

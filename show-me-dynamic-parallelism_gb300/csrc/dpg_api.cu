@@ -45,7 +45,7 @@ namespace dpg_api {
 
 enum Slot {
     S_QV0, S_QV1, S_QSE0, S_QSE1, S_BMP0, S_BMP1, S_CH0, S_CH1, S_QCOUNT, S_CCOUNT, S_LABEL, S_CONTRIB0, S_CONTRIB1, S_RANK0, S_RANK1,
-    S_PARTIAL, S_DPART, S_DFIX, S_DSUM, S_NONSTOP, S_VALS, S_X, S_Y, S_OUTDEG, S_RANKOUT, S_XPERM,
+    S_PARTIAL, S_DPART, S_DFIX, S_DSUM, S_NONSTOP, S_VALS, S_X, S_Y, S_OUTDEG, S_RANKOUT, S_XPERM, S_PENDING,
     S_COUNT_SLOTS
 };
 
@@ -156,6 +156,9 @@ struct dpg_graph {
     int32_t* perm = nullptr;  // old column id -> new
     int32_t* inv = nullptr;   // new -> old
     int32_t* pcol = nullptr;  // col[e] renamed
+    // Transposed CSR (in-arcs), built on first use by colouring.
+    int32_t* t_off = nullptr;
+    int32_t* t_col = nullptr;
 };
 
 namespace dpg_api {
@@ -252,9 +255,12 @@ void graph_free_device(dpg_graph* g) {
     cudaFree(g->perm);
     cudaFree(g->inv);
     cudaFree(g->pcol);
-    g->perm = g->inv = g->pcol = nullptr;
+    cudaFree(g->t_off);
+    cudaFree(g->t_col);
+    g->perm = g->inv = g->pcol = g->t_off = g->t_col = nullptr;
     g->relabel_ready = false;
     cudaFree(g->plan.tiles);
+    cudaFree(g->plan.lane_r0);
     cudaFree(g->plan.hubs_small);
     cudaFree(g->plan.hubs_big);
     g->off = nullptr;
@@ -274,6 +280,7 @@ dpg_status ensure_plan(dpg_graph* g) {
     d.nseg = hp.nseg;
     cudaStream_t s = g->ctx->stream;
     DPG_CUDA_TRY(cudaMalloc(&d.tiles, sizeof(int4) * (hp.tiles.size() + 1)));
+    DPG_CUDA_TRY(cudaMalloc(&d.lane_r0, 32 * (hp.tiles.size() + 1)));
     DPG_CUDA_TRY(cudaMalloc(&d.hubs_small, sizeof(int4) * (hp.hubs_small.size() + 1)));
     DPG_CUDA_TRY(cudaMalloc(&d.hubs_big, sizeof(int4) * (hp.hubs_big.size() + 1)));
     if (!hp.tiles.empty())
@@ -284,6 +291,7 @@ dpg_status ensure_plan(dpg_graph* g) {
     if (!hp.hubs_big.empty())
         DPG_CUDA_TRY(cudaMemcpyAsync(d.hubs_big, hp.hubs_big.data(), sizeof(int4) * hp.hubs_big.size(),
                                      cudaMemcpyHostToDevice, s));
+    DPG_CUDA_TRY(launch_tile_lane_starts(d, g->off, s, g->ctx->sm_count));
     DPG_CUDA_TRY(cudaStreamSynchronize(s));
     g->plan = d;
     g->plan_ready = true;
@@ -326,6 +334,101 @@ dpg_status ensure_relabel(dpg_graph* g) {
     return DPG_OK;
 }
 
+void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const dpg_graph* g);
+
+// Frontier queues, bitmaps and chunk lists from the context arena.
+dpg_status expand_workspace(dpg_ctx* c, int32_t V, int64_t E, int32_t min_chunked, ExpandWorkspace* wsp) {
+    ExpandWorkspace& ws = *wsp;
+    memset(&ws, 0, sizeof(ws));
+    ws.cap_v = static_cast<int64_t>(V) + 1;
+    ws.cap_chunks = expand_chunk_capacity(V, E, min_chunked);
+    ws.bmp_words = (V + 31) / 32 + 1;
+    dpg_status st = DPG_OK;
+    const size_t nv = static_cast<size_t>(ws.cap_v);
+    ws.qv[0] = static_cast<int32_t*>(arena(c, S_QV0, nv * 4, &st));
+    ws.qv[1] = static_cast<int32_t*>(arena(c, S_QV1, nv * 4, &st));
+    ws.qse[0] = static_cast<int2*>(arena(c, S_QSE0, nv * 8, &st));
+    ws.qse[1] = static_cast<int2*>(arena(c, S_QSE1, nv * 8, &st));
+    ws.bmp[0] = static_cast<uint32_t*>(arena(c, S_BMP0, static_cast<size_t>(ws.bmp_words) * 4, &st));
+    ws.bmp[1] = static_cast<uint32_t*>(arena(c, S_BMP1, static_cast<size_t>(ws.bmp_words) * 4, &st));
+    const size_t nc = static_cast<size_t>(ws.cap_chunks);
+    ws.chunks[0] = static_cast<int4*>(arena(c, S_CH0, nc * 16, &st));
+    ws.chunks[1] = static_cast<int4*>(arena(c, S_CH1, nc * 16, &st));
+    ws.qcount = static_cast<uint32_t*>(arena(c, S_QCOUNT, 4 * 4, &st));
+    ws.ccount = static_cast<uint32_t*>(arena(c, S_CCOUNT, 4 * 4, &st));
+    return st;
+}
+
+// In-arc CSR on the device: counts by column histogram, offsets by a host scan, rows filled by an
+// atomic-cursor scatter (row order unspecified, which colouring does not depend on).
+dpg_status ensure_transpose(dpg_graph* g) {
+    if (g->t_off) return DPG_OK;
+    dpg_ctx* c = g->ctx;
+    const size_t nv = static_cast<size_t>(g->V);
+    int32_t* cursor = nullptr;
+    DPG_CUDA_TRY(cudaMalloc(&cursor, (nv + 1) * 4));
+    std::vector<int32_t> h(nv + 1, 0);
+    cudaError_t e = cudaMemsetAsync(cursor, 0, (nv + 1) * 4, c->stream);
+    if (e == cudaSuccess) e = launch_column_histogram(g->col, g->E, cursor, c->stream, c->sm_count);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), cursor, nv * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        cudaFree(cursor);
+        return set_error(DPG_ERR_CUDA, std::string("transpose counts: ") + cudaGetErrorString(e));
+    }
+    int64_t acc = 0;
+    for (size_t v = 0; v < nv; ++v) {
+        const int32_t cnt = h[v];
+        h[v] = static_cast<int32_t>(acc);
+        acc += cnt;
+    }
+    h[nv] = static_cast<int32_t>(acc);
+    e = cudaMalloc(&g->t_off, (nv + 1) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&g->t_col, static_cast<size_t>(g->E > 0 ? g->E : 1) * 4);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g->t_off, h.data(), (nv + 1) * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cursor, h.data(), nv * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = launch_transpose_scatter(g->off, g->col, g->V, cursor, g->t_col, c->stream, c->sm_count);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(cursor);
+    if (e != cudaSuccess) {
+        cudaFree(g->t_off);
+        cudaFree(g->t_col);
+        g->t_off = g->t_col = nullptr;
+        return set_error(DPG_ERR_CUDA, std::string("transpose build: ") + cudaGetErrorString(e));
+    }
+    return DPG_OK;
+}
+
+dpg_status run_color(dpg_ctx* c, dpg_graph* g, const dpg_expand_opts* in_opts, int32_t* d_color) {
+    if (!g || g->ctx != c) return set_error(DPG_ERR_INVALID_ARG, "graph does not belong to this context");
+    if (g->V == 0) return DPG_OK;
+    if (!d_color) return set_error(DPG_ERR_INVALID_ARG, "null output");
+    dpg_expand_opts o;
+    fill_expand_defaults(in_opts, &o, g);
+    DPG_TRY(ensure_transpose(g));
+    ExpandWorkspace ws;
+    dpg_status st = expand_workspace(c, g->V, g->E, o.hub_threshold, &ws);
+    int32_t* pending = static_cast<int32_t*>(arena(c, S_PENDING, static_cast<size_t>(g->V) * 4, &st));
+    if (st != DPG_OK) return st;
+    ExpandLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.off = g->t_off;
+    L.col = g->t_col;
+    L.V = g->V;
+    L.E = g->E;
+    L.label = d_color;
+    L.threshold = o.threshold;
+    L.hub_threshold = o.hub_threshold;
+    L.max_iter = o.max_iterations;
+    L.timeout_ns = static_cast<unsigned long long>(o.timeout_seconds * 1e9);
+    L.trace = c->trace;
+    L.trace_cap = c->trace_cap;
+    c->last_host_iterations = -1;
+    DPG_CUDA_TRY(launch_color(L, g->off, g->col, pending, ws, c->st, c->stream, c->sm_count, &c->last_grid,
+                              &c->last_block, &c->prof));
+    return DPG_OK;
+}
+
 void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const dpg_graph* g) {
     if (in) *o = *in;
     else {
@@ -354,23 +457,7 @@ dpg_status run_expand(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_
         return set_error(DPG_ERR_INVALID_ARG, "unknown solution id");
     const int32_t min_chunked = (o.solution == DPG_SOL_GRID) ? o.threshold : o.hub_threshold;
     ExpandWorkspace ws;
-    memset(&ws, 0, sizeof(ws));
-    ws.cap_v = static_cast<int64_t>(g->V) + 1;
-    ws.cap_chunks = expand_chunk_capacity(g->V, g->E, min_chunked);
-    ws.bmp_words = (g->V + 31) / 32 + 1;
-    dpg_status st = DPG_OK;
-    const size_t nv = static_cast<size_t>(ws.cap_v);
-    ws.qv[0] = static_cast<int32_t*>(arena(c, S_QV0, nv * 4, &st));
-    ws.qv[1] = static_cast<int32_t*>(arena(c, S_QV1, nv * 4, &st));
-    ws.qse[0] = static_cast<int2*>(arena(c, S_QSE0, nv * 8, &st));
-    ws.qse[1] = static_cast<int2*>(arena(c, S_QSE1, nv * 8, &st));
-    ws.bmp[0] = static_cast<uint32_t*>(arena(c, S_BMP0, static_cast<size_t>(ws.bmp_words) * 4, &st));
-    ws.bmp[1] = static_cast<uint32_t*>(arena(c, S_BMP1, static_cast<size_t>(ws.bmp_words) * 4, &st));
-    const size_t nc = static_cast<size_t>(ws.cap_chunks);
-    ws.chunks[0] = static_cast<int4*>(arena(c, S_CH0, nc * 16, &st));
-    ws.chunks[1] = static_cast<int4*>(arena(c, S_CH1, nc * 16, &st));
-    ws.qcount = static_cast<uint32_t*>(arena(c, S_QCOUNT, 4 * 4, &st));
-    ws.ccount = static_cast<uint32_t*>(arena(c, S_CCOUNT, 4 * 4, &st));
+    dpg_status st = expand_workspace(c, g->V, g->E, min_chunked, &ws);
     if (st != DPG_OK) return st;
     ExpandLaunch L;
     L.off = g->off;
@@ -783,6 +870,24 @@ dpg_status dpg_sssp(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_ex
 
 dpg_status dpg_bfs(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_expand_opts* opts, int32_t* h_level) {
     return expand_host(c, g, source, opts, h_level, true);
+}
+
+dpg_status dpg_color_dev(dpg_ctx* c, const dpg_graph* g, const dpg_expand_opts* opts, int32_t* d_color) {
+    DPG_TRY(use_device(c));
+    return run_color(c, const_cast<dpg_graph*>(g), opts, d_color);
+}
+
+dpg_status dpg_color(dpg_ctx* c, const dpg_graph* g, const dpg_expand_opts* opts, int32_t* h_color) {
+    DPG_TRY(use_device(c));
+    if (!g) return set_error(DPG_ERR_INVALID_ARG, "null graph");
+    if (g->V == 0) return DPG_OK;
+    if (!h_color) return set_error(DPG_ERR_INVALID_ARG, "null output");
+    dpg_status st = DPG_OK;
+    int32_t* d = static_cast<int32_t*>(arena(c, S_LABEL, static_cast<size_t>(g->V) * 4, &st));
+    if (!d) return st;
+    DPG_TRY(run_color(c, const_cast<dpg_graph*>(g), opts, d));
+    DPG_CUDA_TRY(cudaMemcpyAsync(h_color, d, static_cast<size_t>(g->V) * 4, cudaMemcpyDeviceToHost, c->stream));
+    return check_device(c);
 }
 
 dpg_status dpg_spmv_f32_dev(dpg_ctx* c, const dpg_graph* g, const float* d_vals, const float* d_x, float* d_y) {

@@ -26,6 +26,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "dpg_kernels.h"
 
 namespace dpg {
@@ -48,10 +50,18 @@ struct ExpandParams {
     DevStatus* st;
     unsigned long long* trace;
     int32_t trace_cap;
+    int32_t* aux;  // colouring: pending lower-neighbour count per vertex
 };
 
+// Operator interface of the expansion:
+//   row_value(u)           value carried with a popped vertex (its label, or its id)
+//   load_edge(e, rv)       neighbour v and candidate value of arc e
+//   want(v, cand, cur)     cheap filter before the atomic (cur = label[v] when kPeek)
+//   commit(v, cand)        the atomic update; true when v must be pushed
 struct SsspOp {
     static constexpr bool kDedup = true;
+    static constexpr bool kPeek = true;
+    __device__ __forceinline__ static int row_value(const ExpandParams& P, int u) { return __ldcg(P.label + u); }
     __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v,
                                                      int& cand) {
         const int2 a = __ldg(P.adj + e);
@@ -60,7 +70,7 @@ struct SsspOp {
     }
     // Read-before-atomic filter (sssp_kernel.cu:55): labels only decrease, so a stale read can only
     // cause an extra atomic, never a missed improvement.
-    __device__ __forceinline__ static bool want(int cand, int cur) { return cand < cur; }
+    __device__ __forceinline__ static bool want(int, int cand, int cur) { return cand < cur; }
     __device__ __forceinline__ static bool commit(const ExpandParams& P, int v, int cand) {
         return cand < atomicMin(P.label + v, cand);
     }
@@ -68,14 +78,35 @@ struct SsspOp {
 
 struct BfsOp {
     static constexpr bool kDedup = false;
+    static constexpr bool kPeek = true;
+    __device__ __forceinline__ static int row_value(const ExpandParams& P, int u) { return __ldcg(P.label + u); }
     __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v,
                                                      int& cand) {
         v = __ldg(P.col + e);
         cand = du + 1;
     }
-    __device__ __forceinline__ static bool want(int, int cur) { return cur == DPG_UNDEFINED_LEVEL; }
+    __device__ __forceinline__ static bool want(int, int, int cur) { return cur == DPG_UNDEFINED_LEVEL; }
     __device__ __forceinline__ static bool commit(const ExpandParams& P, int v, int cand) {
         return atomicCAS(P.label + v, DPG_UNDEFINED_LEVEL, cand) == DPG_UNDEFINED_LEVEL;
+    }
+};
+
+// Greedy colouring (graph_color_kernel.cu:28-49): colour(v) = 1 + max colour of its out-neighbours
+// u < v. The expansion runs over the transposed graph: a coloured u decrements the pending count of
+// every in-neighbour v > u, and the decrement that reaches zero colours v and pushes it.
+struct ColorOp {
+    static constexpr bool kDedup = false;
+    static constexpr bool kPeek = false;
+    __device__ __forceinline__ static int row_value(const ExpandParams&, int u) { return u; }
+    __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int u, int& v, int& cand) {
+        v = __ldg(P.col + e);
+        cand = u;
+    }
+    __device__ __forceinline__ static bool want(int v, int u, int) { return v > u; }
+    __device__ __forceinline__ static bool commit(const ExpandParams& P, int v, int u) {
+        if (atomicSub(P.aux + v, 1) != 1) return false;
+        P.label[v] = __ldcg(P.label + u) + 1;
+        return true;
     }
 };
 
@@ -197,9 +228,9 @@ __device__ __forceinline__ void relax_batch(const ExpandParams& P, const PushCtx
         if (act[u]) Op::load_edge(P, e[u], du[u], v[u], cand[u]);
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) cur[u] = act[u] ? __ldcg(P.label + v[u]) : 0;
+    for (int u = 0; u < U; ++u) cur[u] = (Op::kPeek && act[u]) ? __ldcg(P.label + v[u]) : 0;
 #pragma unroll
-    for (int u = 0; u < U; ++u) ok[u] = act[u] && Op::want(cand[u], cur[u]) && Op::commit(P, v[u], cand[u]);
+    for (int u = 0; u < U; ++u) ok[u] = act[u] && Op::want(v[u], cand[u], cur[u]) && Op::commit(P, v[u], cand[u]);
     push_batch<Op, kClassify, U>(P, Q, ok, v);
 }
 
@@ -355,7 +386,7 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                     const int2 se = __ldcg(qse_cur + i);
                     s = se.x;
                     d = se.y - se.x;
-                    du = __ldcg(P.label + u);
+                    du = Op::row_value(P, u);
                     if (Op::kDedup) __stcg(bmp_cur + (u >> 5), 0u);
                     my_pops += 1;
                     my_edges += static_cast<unsigned long long>(d);
@@ -412,7 +443,7 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                     // Grid-wide consolidation: one chunk (<= 256 arcs) of a chunked vertex.
                     const int4 C = __ldcg(chunks_cur + item);
                     const int v0 = C.x, k0 = C.y, k1 = C.z;
-                    const int du = __ldcg(P.label + v0);
+                    const int du = Op::row_value(P, v0);
                     if (C.w && lane == 0) {
                         if (Op::kDedup) __stcg(bmp_cur + (v0 >> 5), 0u);
                         my_pops += 1;
@@ -441,7 +472,7 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                     const int2 se = __ldcg(qse_cur + i);
                     s = se.x;
                     d = se.y - se.x;
-                    du = __ldcg(P.label + u);
+                    du = Op::row_value(P, u);
                     if (Op::kDedup) __stcg(bmp_cur + (u >> 5), 0u);
                     my_pops += 1;
                     my_edges += static_cast<unsigned long long>(d);
@@ -525,6 +556,28 @@ __global__ void expand_init_kernel(ExpandParams P, int32_t source, int32_t init_
     }
 }
 
+// Colouring start: pending[v] = out-neighbours u < v (with multiplicity); vertices with none take
+// colour 1 and form the first frontier over the transposed graph (P.off / P.col).
+__global__ void color_init_kernel(ExpandParams P, const int32_t* __restrict__ out_off,
+                                  const int32_t* __restrict__ out_col) {
+    const int lane = lane_id();
+    const int64_t wid = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    const PushCtx Q = {P.ws.qv[0], P.ws.qse[0], P.ws.qcount, P.ws.bmp[0], P.ws.chunks[0], P.ws.ccount};
+    for (int64_t base = wid * 32; base < P.V; base += nw * 32) {  // warp-uniform trip count
+        const int v = static_cast<int>(base) + lane;
+        bool ready = false;
+        if (v < P.V) {
+            int pending = 0;
+            for (int e = out_off[v]; e < out_off[v + 1]; ++e) pending += __ldg(out_col + e) < v;
+            P.aux[v] = pending;
+            P.label[v] = pending == 0 ? 1 : 0;
+            ready = pending == 0;
+        }
+        push_converged<ColorOp, true>(P, Q, ready, v < P.V ? v : 0);
+    }
+}
+
 __global__ void barrier_timeout_kernel(DevStatus* st, unsigned long long timeout_ns) {
     if (blockIdx.x == 0 && threadIdx.x == 0) st->bar_count = 0u;
     // Only gridDim.x CTAs exist but the barrier waits for one more: every wait must time out.
@@ -578,6 +631,7 @@ cudaError_t launch_expand(const ExpandLaunch& L, const ExpandWorkspace& ws, DevS
     P.st = st;
     P.trace = L.trace;
     P.trace_cap = L.trace_cap;
+    P.aux = nullptr;
     const int classify = (L.solution == DPG_SOL_GRID || L.solution == DPG_SOL_BINNED) ? 1 : 0;
     const int32_t init_label = L.bfs ? DPG_UNDEFINED_LEVEL : DPG_INF_COST;
     int init_blocks = static_cast<int>((static_cast<int64_t>(L.V) + kBlock - 1) / kBlock);
@@ -586,6 +640,55 @@ cudaError_t launch_expand(const ExpandLaunch& L, const ExpandWorkspace& ws, DevS
     {
         HookScope hs(hook, DPG_KERNEL_INIT, stream);
         expand_init_kernel<<<init_blocks, kBlock, 0, stream>>>(P, L.source, init_label, classify);
+    }
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    void* args[] = {&P};
+    {
+        HookScope hs(hook, DPG_KERNEL_EXPAND, stream);
+        err = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kBlock), args, 0, stream);
+    }
+    if (grid_out) *grid_out = grid;
+    if (block_out) *block_out = kBlock;
+    return err;
+}
+
+cudaError_t launch_color(const ExpandLaunch& L, const int32_t* out_off, const int32_t* out_col, int32_t* pending,
+                         const ExpandWorkspace& ws, DevStatus* st, cudaStream_t stream, int sm_count, int* grid_out,
+                         int* block_out, LaunchHook* hook) {
+    const void* fn = reinterpret_cast<const void*>(expand_kernel<ColorOp, DPG_SOL_BINNED>);
+    int per_sm = 0;
+    cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlock, 0);
+    if (err != cudaSuccess) return err;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int grid = per_sm * sm_count;
+    ExpandParams P;
+    memset(&P, 0, sizeof(P));
+    P.off = L.off;
+    P.col = L.col;
+    P.adj = nullptr;
+    P.label = L.label;
+    P.V = L.V;
+    P.threshold = L.threshold;
+    P.hub_threshold = L.hub_threshold;
+    P.max_iter = L.max_iter;
+    P.timeout_ns = L.timeout_ns;
+    P.ws = ws;
+    P.st = st;
+    P.trace = L.trace;
+    P.trace_cap = L.trace_cap;
+    P.aux = pending;
+    err = cudaMemsetAsync(ws.qcount, 0, sizeof(uint32_t) * 3, stream);
+    if (err == cudaSuccess) err = cudaMemsetAsync(ws.ccount, 0, sizeof(uint32_t) * 3, stream);
+    if (err == cudaSuccess) err = cudaMemsetAsync(&st->bar_count, 0, sizeof(unsigned), stream);
+    if (err == cudaSuccess) err = cudaMemsetAsync(&st->iterations, 0, sizeof(unsigned long long) * 3, stream);
+    if (err != cudaSuccess) return err;
+    int init_blocks = static_cast<int>((static_cast<int64_t>(L.V) + kBlock - 1) / kBlock);
+    if (init_blocks > sm_count * 8) init_blocks = sm_count * 8;
+    if (init_blocks < 1) init_blocks = 1;
+    {
+        HookScope hs(hook, DPG_KERNEL_INIT, stream);
+        color_init_kernel<<<init_blocks, kBlock, 0, stream>>>(P, out_off, out_col);
     }
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;

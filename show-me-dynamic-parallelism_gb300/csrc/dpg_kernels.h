@@ -75,6 +75,12 @@ cudaError_t launch_expand(const ExpandLaunch& L, const ExpandWorkspace& ws, DevS
                           cudaStream_t stream, int sm_count, int* grid_out, int* block_out,
                           LaunchHook* hook);
 
+// Greedy colouring over the transposed graph (L.off / L.col = in-CSR) with the persistent kernel;
+// out_off/out_col is the graph itself, pending a V-int scratch array, L.label the colours.
+cudaError_t launch_color(const ExpandLaunch& L, const int32_t* out_off, const int32_t* out_col, int32_t* pending,
+                         const ExpandWorkspace& ws, DevStatus* st, cudaStream_t stream, int sm_count, int* grid_out,
+                         int* block_out, LaunchHook* hook);
+
 // Grid barrier with one CTA missing: its bounded waits must run out (failure-detection test).
 cudaError_t launch_barrier_timeout_test(DevStatus* st, unsigned long long timeout_ns,
                                         cudaStream_t stream);
@@ -99,6 +105,7 @@ void build_row_plan(const int32_t* offsets, int32_t V, RowPlanHost* plan);
 
 struct RowPlanDev {
     int4* tiles = nullptr;
+    uint8_t* lane_r0 = nullptr;  // [ntiles][32] merge-path start row of each lane (normal tiles)
     int32_t ntiles = 0;
     int4* hubs_small = nullptr;
     int32_t nhub_small = 0;
@@ -139,8 +146,15 @@ cudaError_t launch_relabel_columns(const int32_t* col, const int32_t* perm, int6
                                    int sm_count);
 cudaError_t launch_gather_by_index(const float* x, const int32_t* inv, int32_t V, float* out, cudaStream_t s,
                                    int sm_count);
+// Transposed CSR on the device: t_col[t_off[v] .. t_off[v+1]) lists the u with v in row u (order
+// within a row unspecified); cursor is V ints of scratch holding t_off[0..V).
+cudaError_t launch_transpose_scatter(const int32_t* off, const int32_t* col, int32_t V, int32_t* cursor,
+                                     int32_t* t_col, cudaStream_t s, int sm_count);
 // perm[old] = new, inv[new] = old; most frequent columns first (by bit length of the count), ties by id.
 void frequency_order(const int32_t* counts, int32_t V, int32_t* perm, int32_t* inv);
+
+// Fills plan.lane_r0 from the tiles and the offsets (once per graph).
+cudaError_t launch_tile_lane_starts(const RowPlanDev& plan, const int32_t* off, cudaStream_t s, int sm_count);
 
 // Grid shape used by the row-gather kernels (needed to size dpart/dfix).
 void rowgather_grid(int sm_count, int* gather_blocks, int* fix_blocks, int* block_threads);

@@ -42,7 +42,28 @@ __global__ void gather_by_index_kernel(const float* __restrict__ x, const int32_
         out[i] = __ldg(x + __ldg(inv + i));
 }
 
+// Warp per row; each lane claims a slot of the target's in-row.
+__global__ void transpose_scatter_kernel(const int32_t* __restrict__ off, const int32_t* __restrict__ col, int32_t V,
+                                         int32_t* cursor, int32_t* __restrict__ t_col) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t u = w; u < V; u += nw) {
+        const int b = __ldg(off + u), e = __ldg(off + u + 1);
+        for (int k = b + lane; k < e; k += 32) {
+            const int v = __ldg(col + k);
+            t_col[atomicAdd(cursor + v, 1)] = static_cast<int32_t>(u);
+        }
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_transpose_scatter(const int32_t* off, const int32_t* col, int32_t V, int32_t* cursor,
+                                     int32_t* t_col, cudaStream_t s, int sm_count) {
+    if (V > 0) transpose_scatter_kernel<<<sm_count * 8, 256, 0, s>>>(off, col, V, cursor, t_col);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_column_histogram(const int32_t* col, int64_t E, int32_t* counts, cudaStream_t s, int sm_count) {
     if (E > 0) column_histogram_kernel<<<sm_count * 8, 256, 0, s>>>(col, E, counts);

@@ -55,16 +55,20 @@ __device__ __forceinline__ float load_product(const RowGatherLaunch& L, const fl
 }
 
 // PageRank epilogue of one row: new rank, next contribution, dangling mass, convergence flag.
-__device__ __forceinline__ void pr_epilogue(const RowGatherLaunch& L, int v, float sum, float base,
+// od / pos are the row's out-degree and contribution slot (perm[v] with renamed columns).
+__device__ __forceinline__ void pr_epilogue(const RowGatherLaunch& L, int v, float sum, float base, int od, int pos,
                                             double& dang) {
     const float nv = fmaf(L.damping, sum, base);
     if (L.rank_out) L.rank_out[v] = nv;
     if (L.rank_prev && fabsf(nv - __ldg(L.rank_prev + v)) > L.epsilon) *L.nonstop = 1u;
-    const int od = __ldg(L.outdeg + v);
     // Only vertices with out-arcs are ever gathered (they are the columns), so dangling vertices
     // write no contribution at all.
-    if (od > 0) L.y[L.perm ? __ldg(L.perm + v) : v] = nv / static_cast<float>(od);
+    if (od > 0) L.y[pos] = nv / static_cast<float>(od);
     else dang += static_cast<double>(nv);
+}
+
+__device__ __forceinline__ void pr_epilogue(const RowGatherLaunch& L, int v, float sum, float base, double& dang) {
+    pr_epilogue(L, v, sum, base, __ldg(L.outdeg + v), L.perm ? __ldg(L.perm + v) : v, dang);
 }
 
 __device__ __forceinline__ float pr_base(const RowGatherLaunch& L) {
@@ -88,8 +92,15 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
     if (MODE == kModePagerank) base = pr_base(L);
     double dang = 0.0;
 
-    for (int t = gwarp; t < L.plan.ntiles; t += nwarps) {
-        const int4 T = __ldg(L.plan.tiles + t);
+    // Each warp walks its tiles with the next descriptor and lane starts already in flight.
+    const int ntiles = L.plan.ntiles;
+    int t = gwarp;
+    int4 T = t < ntiles ? __ldg(L.plan.tiles + t) : make_int4(0, 0, 0, 0);
+    int r0 = t < ntiles ? __ldg(L.plan.lane_r0 + t * 32 + lane) : 0;
+    for (; t < ntiles; t += nwarps) {
+        const int tn = t + nwarps;
+        const int4 Tn = tn < ntiles ? __ldg(L.plan.tiles + tn) : make_int4(0, 0, 0, 0);
+        const int r0n = tn < ntiles ? __ldg(L.plan.lane_r0 + tn * 32 + lane) : 0;
         const int row = T.x, nrows = T.y, nb = T.z, nnz = T.w;
         if (nrows < 0) {
             // Hub segment: fixed-order lane sums, then a butterfly; partial goes to the fix-up.
@@ -101,7 +112,15 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
             }
             acc = warp_sum_f32(acc);
             if (lane == 0) L.partial[-(nrows + 1)] = acc;
+            T = Tn;
+            r0 = r0n;
             continue;
+        }
+        // Epilogue inputs of the first 32 rows, requested before the gathers.
+        int od0 = 0, pos0 = 0;
+        if (MODE == kModePagerank && lane < nrows) {
+            od0 = __ldg(L.outdeg + row + lane);
+            pos0 = L.perm ? __ldg(L.perm + row + lane) : row + lane;
         }
         // Stage relative row ends and products.
         for (int r = lane; r < nrows; r += 32) re[pad(r)] = __ldg(L.off + row + r + 1) - nb;
@@ -121,34 +140,30 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
             }
         }
         __syncwarp();
-        // Merge-path: lane owns merge items [d0, d1). r = row ends consumed, k = nonzeros consumed.
+        // Merge-path: lane owns merge items [d0, d1) starting at row r0 (precomputed per tile);
+        // r = row ends consumed, k = nonzeros consumed. The walk is branch-free.
         const int total = nrows + nnz;
         const int d0 = min(lane * kIpl, total);
         const int d1 = min(d0 + kIpl, total);
-        int lo = max(0, d0 - nnz), hi = min(d0, nrows);
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (re[pad(mid - 1)] + mid <= d0) lo = mid;
-            else hi = mid - 1;
-        }
-        int r = lo, k = d0 - lo;
+        int r = d0 < total ? r0 : nrows;
+        int k = d0 - r;
         float acc = 0.0f;
         int first_emit = -1;
         int rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
 #pragma unroll
         for (int i = 0; i < kIpl; ++i) {
-            if (d0 + i < d1) {
-                if (k < rend) {
-                    acc += val[pad(k)];
-                    ++k;
-                } else {
-                    if (first_emit < 0) first_emit = r;
-                    out[pad(r)] = acc;
-                    acc = 0.0f;
-                    ++r;
-                    rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
-                }
+            const bool live = d0 + i < d1;
+            const bool take = live && k < rend;
+            const bool emit = live && !(k < rend);
+            const float v = val[pad(k)];  // k <= nnz <= 255 stays inside the padded row
+            if (emit) {
+                out[pad(r)] = acc;
+                first_emit = first_emit < 0 ? r : first_emit;
             }
+            acc = take ? acc + v : (emit ? 0.0f : acc);
+            k += take ? 1 : 0;
+            r += emit ? 1 : 0;
+            if (emit) rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
         }
         // Segmented inclusive scan of the lanes' open partials (key = row still open at lane end).
         float cv = acc;
@@ -167,11 +182,15 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
             const float sum = out[pad(rr)];
             if (MODE == kModeSpmv) {
                 L.y[row + rr] = sum;
+            } else if (rr < 32) {
+                pr_epilogue(L, row + rr, sum, base, od0, pos0, dang);
             } else {
                 pr_epilogue(L, row + rr, sum, base, dang);
             }
         }
         __syncwarp();
+        T = Tn;
+        r0 = r0n;
     }
     if (MODE == kModePagerank) {
         dang = warp_sum_f64(dang);
@@ -250,7 +269,38 @@ __global__ void __launch_bounds__(kInitBlock) pr_init_kernel(RowGatherLaunch L, 
     if (lane == 0) L.dpart[gwarp] = dang;
 }
 
+// Merge-path start row of each lane of each normal tile, once per graph: the largest r with
+// (row end r-1) + r <= 8 * lane, i.e. the row ends the lane's first merge item comes after.
+__global__ void tile_lane_starts_kernel(const int4* __restrict__ tiles, int ntiles, const int32_t* __restrict__ off,
+                                        uint8_t* __restrict__ lane_r0) {
+    const int lane = threadIdx.x & 31;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int t = w; t < ntiles; t += nw) {
+        const int4 T = __ldg(tiles + t);
+        int lo = 0;
+        if (T.y > 0) {
+            const int row = T.x, nrows = T.y, nb = T.z, nnz = T.w;
+            const int total = nrows + nnz;
+            const int d0 = min(lane * kIpl, total);
+            lo = max(0, d0 - nnz);
+            int hi = min(d0, nrows);
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (__ldg(off + row + mid) - nb + mid <= d0) lo = mid;
+                else hi = mid - 1;
+            }
+        }
+        lane_r0[static_cast<int64_t>(t) * 32 + lane] = static_cast<uint8_t>(lo > 255 ? 255 : lo);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_tile_lane_starts(const RowPlanDev& plan, const int32_t* off, cudaStream_t s, int sm_count) {
+    if (plan.ntiles > 0) tile_lane_starts_kernel<<<sm_count * 8, 256, 0, s>>>(plan.tiles, plan.ntiles, off, plan.lane_r0);
+    return cudaGetLastError();
+}
 
 void rowgather_grid(int sm_count, int* gather_blocks, int* fix_blocks, int* block_threads) {
     *gather_blocks = sm_count;
