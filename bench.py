@@ -47,7 +47,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["dpg", "reference"], default="dpg")
     ap.add_argument("--no-extra", action="store_true", help="skip the SpMV / SSSP / BFS side measurements")
-    ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs"], default="pagerank",
+    ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs", "adjoint", "prgrad"], default="pagerank",
                     help="pagerank is the headline; the others print their own line (used for profiling)")
     ap.add_argument("--scale", type=int, default=0, help="R-MAT scale for --workload spmv/sssp/bfs")
     ap.add_argument("--no-relabel", action="store_true", help="turn off the column renaming of SpMV/PageRank")
@@ -262,9 +262,111 @@ def measure_expand(dpg, ctx, torch, g, peak, kind, nsrc=4, seed=24):
             "sources": srcs}
 
 
+def measure_adjoint(dpg, ctx, torch, g, peak, nrhs=64, reps=5):
+    """SpMV backward on g with lognormal(0,1) FP32 values and nrhs right-hand sides: the batched call
+    (dX = A^T G and dA together) against looping the plain single-vector kernels once per column."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    V, E = g.V, g.E
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(5)
+    vals = torch.exp(torch.randn(E, device=dev, generator=gen))
+    X = torch.rand((V, nrhs), device=dev, generator=gen) * 2 - 1
+    G = torch.rand((V, nrhs), device=dev, generator=gen) * 2 - 1
+    dX = torch.empty((V, nrhs), device=dev)
+    dA = torch.empty(E, device=dev)
+    dg = dpg.Graph(ctx, g.offsets, g.col)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def batched():
+        dpg.spmv_bwd_dev(ctx, dg, vals.data_ptr(), nrhs, X.data_ptr(), G.data_ptr(), dX.data_ptr(), dA.data_ptr())
+
+    # Plain kernels per column: dX[:, j] = A^T G[:, j] by the row-gather SpMV on the transposed graph
+    # (values permuted once, outside the loop), dA += G[row, j] * X[col, j] by the arc kernel.
+    t_off, t_col, t_arc = dpg.csr_transpose_perm(V, g.offsets, g.col)
+    gT = dpg.Graph(ctx, t_off, t_col)
+    vals_t = vals[torch.from_numpy(t_arc.astype(np.int64)).to(dev)].contiguous()
+    Xc, Gc = X.t().contiguous(), G.t().contiguous()
+    dXc = torch.empty((nrhs, V), device=dev)
+    dA1 = torch.empty(E, device=dev)
+    dA_loop = torch.empty(E, device=dev)
+
+    def looped():
+        dA_loop.zero_()
+        for j in range(nrhs):
+            dpg.spmv_dev(ctx, gT, vals_t.data_ptr(), Gc[j].data_ptr(), dXc[j].data_ptr())
+            dpg.spmv_bwd_dev(ctx, dg, vals.data_ptr(), 1, Xc[j].data_ptr(), Gc[j].data_ptr(), None, dA1.data_ptr())
+            dA_loop.add_(dA1)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_b = timed(batched)
+    t_l = timed(looped)
+    # Agreement is judged against the magnitude bound |A|^T |G| (and |G[row]|.|X[col]| for dA): the two
+    # arms sum in different orders, and hub columns of the transpose cancel heavily.
+    dX_b, dA_b = dX.clone(), dA.clone()
+    Xa, Ga, va = X.abs(), G.abs(), vals.abs()
+    dpg.spmv_bwd_dev(ctx, dg, va.data_ptr(), nrhs, Xa.data_ptr(), Ga.data_ptr(), dX.data_ptr(), dA.data_ptr())
+    torch.cuda.synchronize()
+    err_x = float(((dX_b.t() - dXc).abs() / (dX.t() + 1e-30)).max())
+    err_a = float(((dA_b - dA_loop).abs() / (dA + 1e-30)).max())
+    ok = err_x < 1e-5 and err_a < 1e-5
+    bytes_bwd = 4 * (V + 1) + 8 * E + 4 * nrhs * V * 3 + 4 * E
+    return {"nrhs": nrhs, "batched_ms": t_b, "looped_ms": t_l, "speedup": t_l / t_b,
+            "batched_gteps": E * nrhs / (t_b / 1e3) / 1e9, "roofline_frac": bytes_bwd / (t_b / 1e3) / 1e9 / peak,
+            "bytes_per_call": bytes_bwd, "results_agree": ok, "max_err_dx_over_bound": err_x,
+            "max_err_da_over_bound": err_a}
+
+
+def measure_prgrad(dpg, ctx, torch, g, peak, reps=3):
+    """Weighted PageRank gradient on g (out-adjacency) with lognormal(0,1) FP32 weights and the loss
+    sum of r over a seeded random 1% vertex subset: forward to a relative change of 3e-7, the
+    adjoint fixed point to the same tolerance, and the per-arc gradient, against the forward alone."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    V, E = g.V, g.E
+    rng = np.random.default_rng(20)
+    w = torch.from_numpy(np.exp(rng.standard_normal(E)).astype(np.float32)).to(dev)
+    seed_np = np.zeros(V, np.float32)
+    seed_np[rng.choice(V, max(1, V // 100), replace=False)] = 1.0
+    seed = torch.from_numpy(seed_np).to(dev)
+    zero = torch.zeros(V, device=dev)
+    r = torch.empty(V, device=dev)
+    gr = torch.empty(E, device=dev)
+    dg = dpg.Graph(ctx, g.offsets, g.col)
+    opts = dict(damping=0.85, total_rank=1.0, iterations=2000, epsilon=3e-7, adjoint_epsilon=3e-7)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(sd):
+        dpg.pagerank_grad_dev(ctx, dg, w.data_ptr(), sd.data_ptr(), r.data_ptr(), gr.data_ptr(), **opts)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0.record()
+            sw = dpg.pagerank_grad_dev(ctx, dg, w.data_ptr(), sd.data_ptr(), r.data_ptr(), gr.data_ptr(), **opts)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return min(ts), sw
+
+    t_fwd, (nf, _) = timed(zero)   # zero seed: the adjoint loop stops after one sweep
+    t_all, (nf2, na) = timed(seed)
+    sweeps = nf2 + na + 2
+    return {"ms_total": t_all, "ms_forward_only": t_fwd, "forward_sweeps": nf2, "adjoint_sweeps": na,
+            "ms_per_sweep": t_all / sweeps, "gteps_sweeps": sweeps * E / (t_all / 1e3) / 1e9,
+            "grad_over_forward": t_all / t_fwd, "rank_sum": float(r.double().sum())}
+
+
 def extra_measurements(dpg, ctx, torch, g, peak, steps):
     """SpMV on the scale-22 graph; SSSP and BFS on R-MAT scale 24 (device-resident, CUDA events)."""
     out = {"spmv_rmat22": measure_spmv(dpg, ctx, torch, g, peak, steps)}
+    out["spmv_bwd_rmat22_64rhs"] = measure_adjoint(dpg, ctx, torch, g, peak)
     g24 = dpg.rmat_csr(24, 16, seed=24, wmin=1, wmax=255)
     out["sssp_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "sssp")
     out["bfs_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "bfs")
@@ -285,10 +387,19 @@ def run_single_workload(args):
     peak, peak_kind = measured_peaks()
     ctx = dpg.Context(0)
     ctx.set_stream(stream.cuda_stream)
-    if args.workload == "spmv":
+    if args.workload == "prgrad":
+        scale = args.scale or 20
+        g = dpg.rmat_csr(scale, 16, seed=scale, weights=False)
+        res = measure_prgrad(dpg, ctx, torch, g, peak)
+        res["gteps"] = res["gteps_sweeps"]
+    elif args.workload in ("spmv", "adjoint"):
         scale = args.scale or 22
         g = dpg.rmat_csr(scale, 16, seed=scale, weights=False)
-        res = measure_spmv(dpg, ctx, torch, g, peak, args.steps, relabel=not args.no_relabel)
+        if args.workload == "spmv":
+            res = measure_spmv(dpg, ctx, torch, g, peak, args.steps, relabel=not args.no_relabel)
+        else:
+            res = measure_adjoint(dpg, ctx, torch, g, peak)
+            res["gteps"] = res["batched_gteps"]
     else:
         scale = args.scale or 24
         g = dpg.rmat_csr(scale, 16, seed=scale, wmin=1, wmax=255)

@@ -151,6 +151,34 @@ dpg_status dpg_spmv_f32(dpg_ctx* ctx, const dpg_graph* g, const float* h_vals, c
 dpg_status dpg_spmv_f32_dev(dpg_ctx* ctx, const dpg_graph* g, const float* d_vals,
                             const float* d_x, float* d_y);
 
+/* ---- batched right-hand sides and the SpMV adjoint (no counterpart in the reference) ------------ */
+/* Row-major blocks of nrhs columns (1 <= nrhs <= 128): X, G, Y, dX are [V][nrhs] FP32.
+ *   dpg_spmm_f32_dev:      Y = A X, A = g with values vals[E] in CSR order
+ *   dpg_spmv_bwd_f32_dev:  dX = A^T G and dA[e] = sum_j G[row(e)][j] * X[col(e)][j]
+ * Sums run in a fixed order (A^T through the transposed CSR in invertGraph order, built once per
+ * graph on first use), so results are bit-reproducible. d_dX or d_dA may be NULL to skip one. */
+dpg_status dpg_spmm_f32_dev(dpg_ctx* ctx, const dpg_graph* g, const float* d_vals, int32_t nrhs, const float* d_X,
+                            float* d_Y);
+dpg_status dpg_spmv_bwd_f32_dev(dpg_ctx* ctx, const dpg_graph* g, const float* d_vals, int32_t nrhs,
+                                const float* d_X, const float* d_G, float* d_dX, float* d_dA);
+
+/* ---- weighted PageRank and its gradient w.r.t. the edge weights (no counterpart in the reference) */
+/* g is the out-adjacency; arc e = (u -> col[e]) has weight w[e] >= 0 and W[u] = sum of u's weights
+ * (u dangling when W[u] == 0). r is the fixed point of
+ *     r[v] = (1-d) T / V + d D / V + d * sum_{u->v} w[e] r[u] / W[u],   D = sum of dangling r,
+ * with d = opts->damping and T = opts->total_rank, run from T / V (0 with init_zero) until no rank
+ * changes by more than opts->epsilon times its new value (a relative test; with epsilon <= 0 for
+ * exactly opts->iterations sweeps). d_seed = dL/dr (V floats). The adjoint
+ * lambda = s + d P lambda (dangling rows d/V * sum lambda) is solved the same way with relative
+ * tolerance adjoint_epsilon, and
+ *     d_grad[e] = dL/dw[e] = d * r[u] / W[u] * (lambda[col[e]] - sum_t w[e'] lambda[t] / W[u]).
+ * opts->iterations caps each of the two loops (0 with a tolerance: 10000 sweeps at most).
+ * Outputs: d_rank (V), d_grad (E). The pull sweeps use the transposed CSR, built once per graph. */
+dpg_status dpg_pagerank_grad_f32_dev(dpg_ctx* ctx, const dpg_graph* g, const float* d_weights, const float* d_seed,
+                                     const dpg_pr_opts* opts, double adjoint_epsilon, float* d_rank, float* d_grad);
+/* Forward and adjoint sweeps of the last dpg_pagerank_grad_f32_dev call on ctx. */
+dpg_status dpg_ctx_grad_sweeps(const dpg_ctx* ctx, int64_t* forward, int64_t* adjoint);
+
 /* ---- PageRank pull (replaces PAGERANK_GPU / pg_pull_gpu, pagerank_wrapper.cu:199-244,366-400) -- */
 /* g_in is the transposed CSR (childVertexArray/rEdgeArray of invertGraph, global.cpp:237-277);
  * outdeg[v] is the out-degree in the original graph (outdegreeArray, pagerank.cpp:108-113). */
@@ -235,6 +263,9 @@ dpg_status dpg_csr_from_arcs(int32_t V, int64_t E, const int32_t* src, const int
 /* invertGraph (global.cpp:237-277): transposed CSR in the reference's neighbour order. */
 dpg_status dpg_csr_transpose(int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
                              int32_t* in_offsets, int32_t* in_col);
+/* Same, and in_arc[p] = index in col of the arc that transposed slot p came from. */
+dpg_status dpg_csr_transpose_perm(int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
+                                  int32_t* in_offsets, int32_t* in_col, int32_t* in_arc);
 /* Writes a DIMACS9 .gr file: "p sp V E", optional "s", then "a u v w" lines in arc order. */
 dpg_status dpg_write_dimacs9(const char* path, int32_t V, int64_t E, const int32_t* src,
                              const int32_t* dst, const int32_t* w, int32_t source);

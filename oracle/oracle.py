@@ -224,6 +224,68 @@ def color(off, col) -> tuple[np.ndarray, int]:
     return c[:V], int(n)
 
 
+# ------------------------------------------- weighted PageRank and its edge-weight gradient (FP64) --
+# No counterpart in the reference; restated from the fixed-point equations that
+# dpg_pagerank_grad_f32_dev documents, and checked against central differences of the forward map.
+def _weighted_operator(off, col, w):
+    import scipy.sparse as sp
+
+    off = np.asarray(off, np.int64)
+    V = off.shape[0] - 1
+    # Copies: scipy may canonicalise (sum duplicate arcs) in place on the arrays it is given.
+    A = sp.csr_matrix((np.asarray(w, np.float64).copy(), np.asarray(col, np.int64).copy(), off.copy()), shape=(V, V))
+    W = np.zeros(V)
+    np.add.at(W, np.repeat(np.arange(V), np.diff(off)), np.asarray(w, np.float64))
+    return A, W
+
+
+def pagerank_weighted_f64(off, col, w, damping=0.85, total=1.0, init_zero=False, iterations=5000, epsilon=1e-15):
+    """r[v] = (1-d)T/V + d D/V + d sum_{u->v} w r[u]/W[u]; sweeps until every |change| <= epsilon * |r|.
+    Returns (r, sweeps)."""
+    A, W = _weighted_operator(off, col, w)
+    V = W.shape[0]
+    AT = A.T.tocsr()
+    dang = W == 0
+    Wn = np.where(dang, 1.0, W)
+    r = np.zeros(V) if init_zero else np.full(V, total / V)
+    sweeps = 0
+    for _ in range(iterations):
+        contrib = np.where(dang, 0.0, r / Wn)
+        rn = (1 - damping) * total / V + damping * r[dang].sum() / V + damping * (AT @ contrib)
+        sweeps += 1
+        done = bool(np.all(np.abs(rn - r) <= epsilon * np.abs(rn)))
+        r = rn
+        if epsilon > 0 and done:
+            break
+    return r, sweeps
+
+
+def pagerank_weighted_grad_f64(off, col, w, seed, damping=0.85, total=1.0, iterations=5000, epsilon=1e-15):
+    """(r, lambda, dL/dw) for seed = dL/dr, by the adjoint fixed point
+    lambda[u] = s[u] + d/W[u] sum_{u->t} w lambda[t] (dangling: s[u] + d/V sum lambda)."""
+    off = np.asarray(off, np.int64)
+    col = np.asarray(col, np.int64)
+    r, _ = pagerank_weighted_f64(off, col, w, damping, total, False, iterations, epsilon)
+    A, W = _weighted_operator(off, col, w)
+    V = W.shape[0]
+    dang = W == 0
+    Wn = np.where(dang, 1.0, W)
+    s = np.asarray(seed, np.float64)
+    lam = s.copy()
+    for _ in range(iterations):
+        y = A @ lam
+        ln = s + np.where(dang, damping / V * lam.sum(), damping * y / Wn)
+        done = bool(np.all(np.abs(ln - lam) <= epsilon * np.abs(ln)))
+        lam = ln
+        if epsilon > 0 and done:
+            break
+    q = np.where(dang, 0.0, (A @ lam) / Wn)
+    rows = np.repeat(np.arange(V), np.diff(off))
+    c = np.where(dang, 0.0, damping * r / Wn)
+    grad = c[rows] * (lam[col] - q[rows])
+    return r, lam, grad
+
+
 # ----------------------------------------------------------------- the reference's own host code --
 def ref_load(path, fmt=0):
     """The reference loader itself: returns (V, E, source, off, col, w, in_off, in_col)."""

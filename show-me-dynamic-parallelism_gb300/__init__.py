@@ -146,6 +146,11 @@ _SIGS = {
     "dpg_host_graph_free": [POINTER(_HostGraph)],
     "dpg_csr_from_arcs": [c_int32, c_int64, _P, _P, _P, _P, _P, _P],
     "dpg_csr_transpose": [c_int32, c_int64, _P, _P, _P, _P],
+    "dpg_csr_transpose_perm": [c_int32, c_int64, _P, _P, _P, _P, _P],
+    "dpg_spmm_f32_dev": [_P, _P, _P, c_int32, _P, _P],
+    "dpg_spmv_bwd_f32_dev": [_P, _P, _P, c_int32, _P, _P, _P, _P],
+    "dpg_pagerank_grad_f32_dev": [_P, _P, _P, _P, _P, c_double, _P, _P],
+    "dpg_ctx_grad_sweeps": [_P, POINTER(c_int64), POINTER(c_int64)],
     "dpg_write_dimacs9": [c_char_p, c_int32, c_int64, _P, _P, _P, c_int32],
     "dpg_write_cost": [c_char_p, c_int32, c_int32, _P],
     "dpg_write_level": [c_char_p, c_int32, _P],
@@ -481,6 +486,42 @@ def spmv(ctx: Context, g: Graph, vals, x) -> np.ndarray:
     y = np.empty(max(g.V, 1), np.float32)
     _check(lib().dpg_spmv_f32(ctx.handle, g.handle, _ptr(v), _ptr(xx), _ptr(y)))
     return y[:g.V]
+
+
+def spmm_dev(ctx: Context, g: Graph, d_vals: int, nrhs: int, d_X: int, d_Y: int) -> None:
+    """Y = A X for nrhs row-major columns (device pointers)."""
+    _check(lib().dpg_spmm_f32_dev(ctx.handle, g.handle, c_void_p(d_vals), nrhs, c_void_p(d_X), c_void_p(d_Y)))
+
+
+def spmv_bwd_dev(ctx: Context, g: Graph, d_vals: int, nrhs: int, d_X: int | None, d_G: int, d_dX: int | None,
+                 d_dA: int | None) -> None:
+    """dX = A^T G and dA[e] = <G[row(e)], X[col(e)]> (device pointers; None skips an output)."""
+    _check(lib().dpg_spmv_bwd_f32_dev(ctx.handle, g.handle, c_void_p(d_vals), nrhs,
+                                      c_void_p(d_X) if d_X else None, c_void_p(d_G),
+                                      c_void_p(d_dX) if d_dX else None, c_void_p(d_dA) if d_dA else None))
+
+
+def pagerank_grad_dev(ctx: Context, g: Graph, d_weights: int, d_seed: int, d_rank: int, d_grad: int,
+                      adjoint_epsilon: float = 0.0, **opts) -> tuple[int, int]:
+    """Weighted PageRank r on the out-adjacency g and dL/dw for the seed dL/dr (device pointers).
+    Returns (forward sweeps, adjoint sweeps)."""
+    o = pr_opts(**opts)
+    _check(lib().dpg_pagerank_grad_f32_dev(ctx.handle, g.handle, c_void_p(d_weights), c_void_p(d_seed), byref(o),
+                                           float(adjoint_epsilon), c_void_p(d_rank), c_void_p(d_grad)))
+    f, a = c_int64(0), c_int64(0)
+    _check(lib().dpg_ctx_grad_sweeps(ctx.handle, byref(f), byref(a)))
+    return int(f.value), int(a.value)
+
+
+def csr_transpose_perm(V: int, offsets, col):
+    """invertGraph order plus in_arc[p] = index of the arc that transposed slot p came from."""
+    offsets, col = _i32(offsets), _i32(col)
+    E = int(col.shape[0])
+    in_off = np.empty(V + 1, np.int32)
+    in_col = np.empty(max(E, 1), np.int32)
+    in_arc = np.empty(max(E, 1), np.int32)
+    _check(lib().dpg_csr_transpose_perm(V, E, _ptr(offsets), _ptr(col), _ptr(in_off), _ptr(in_col), _ptr(in_arc)))
+    return in_off, in_col[:E], in_arc[:E]
 
 
 def spmv_dev(ctx: Context, g: Graph, d_vals: int, d_x: int, d_y: int) -> None:

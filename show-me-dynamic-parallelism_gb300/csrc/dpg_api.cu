@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -45,7 +46,8 @@ namespace dpg_api {
 
 enum Slot {
     S_QV0, S_QV1, S_QSE0, S_QSE1, S_BMP0, S_BMP1, S_CH0, S_CH1, S_QCOUNT, S_CCOUNT, S_LABEL, S_CONTRIB0, S_CONTRIB1, S_RANK0, S_RANK1,
-    S_PARTIAL, S_DPART, S_DFIX, S_DSUM, S_NONSTOP, S_VALS, S_X, S_Y, S_OUTDEG, S_RANKOUT, S_XPERM, S_PENDING,
+    S_PARTIAL, S_DPART, S_DFIX, S_DSUM, S_NONSTOP, S_VALS, S_X, S_Y, S_OUTDEG, S_RANKOUT, S_XPERM, S_PENDING, S_SPMM_PARTIAL, S_VALS_T,
+    S_PRG_W, S_PRG_Y, S_PRG_C, S_PRG_V0, S_PRG_V1, S_PRG_V2, S_PRG_V3, S_PRG_PART, S_PRG_RED, S_PRG_FLAGS,
     S_COUNT_SLOTS
 };
 
@@ -132,6 +134,7 @@ struct dpg_ctx {
     Buf bufs[S_COUNT_SLOTS];
     int last_grid = 0;
     int last_block = 0;
+    int64_t last_grad_sweeps[2] = {0, 0};  // forward and adjoint sweeps of the last PageRank gradient
     int64_t last_host_iterations = -1;  // PageRank sweeps (host-counted); -1: read from the device
     Profiler prof;
     unsigned long long* trace = nullptr;  // per-iteration expansion trace (dpg_ctx_trace_enable)
@@ -159,6 +162,17 @@ struct dpg_graph {
     // Transposed CSR (in-arcs), built on first use by colouring.
     int32_t* t_off = nullptr;
     int32_t* t_col = nullptr;
+    // Batched-RHS plans: over the graph's rows, and over the transposed CSR in invertGraph order
+    // (tt_*, with tt_arc[p] = the arc that transposed slot p came from), built on first use.
+    bool spmm_ready = false;
+    SpmmPlanDev spmm_plan;
+    bool spmm_t_ready = false;
+    SpmmPlanDev spmm_t_plan;
+    int32_t* tt_col = nullptr;
+    int32_t* tt_arc = nullptr;
+    // The same transposed CSR as a graph of its own (row-gather plan, column renaming), for pull
+    // sweeps over in-arcs with permuted arc values; built on first use by the weighted PageRank.
+    dpg_graph* tgraph = nullptr;
 };
 
 namespace dpg_api {
@@ -249,6 +263,11 @@ dpg_status graph_finish(dpg_ctx* c, dpg_graph* g, const int32_t* d_w_src) {
 }
 
 void graph_free_device(dpg_graph* g) {
+    if (g->tgraph) {
+        graph_free_device(g->tgraph);
+        delete g->tgraph;
+        g->tgraph = nullptr;
+    }
     cudaFree(g->off);
     cudaFree(g->col);
     cudaFree(g->adj);
@@ -258,6 +277,15 @@ void graph_free_device(dpg_graph* g) {
     cudaFree(g->t_off);
     cudaFree(g->t_col);
     g->perm = g->inv = g->pcol = g->t_off = g->t_col = nullptr;
+    for (SpmmPlanDev* p : {&g->spmm_plan, &g->spmm_t_plan}) {
+        cudaFree(p->items);
+        cudaFree(p->hubs);
+        *p = SpmmPlanDev();
+    }
+    cudaFree(g->tt_col);
+    cudaFree(g->tt_arc);
+    g->tt_col = g->tt_arc = nullptr;
+    g->spmm_ready = g->spmm_t_ready = false;
     g->relabel_ready = false;
     cudaFree(g->plan.tiles);
     cudaFree(g->plan.lane_r0);
@@ -335,6 +363,66 @@ dpg_status ensure_relabel(dpg_graph* g) {
 }
 
 void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const dpg_graph* g);
+
+dpg_status upload_spmm_plan(dpg_ctx* c, const SpmmPlanHost& hp, SpmmPlanDev* d) {
+    d->nitems = static_cast<int32_t>(hp.items.size());
+    d->nhubs = static_cast<int32_t>(hp.hubs.size());
+    d->nseg = hp.nseg;
+    DPG_CUDA_TRY(cudaMalloc(&d->items, sizeof(int4) * (hp.items.size() + 1)));
+    DPG_CUDA_TRY(cudaMalloc(&d->hubs, sizeof(int4) * (hp.hubs.size() + 1)));
+    if (!hp.items.empty())
+        DPG_CUDA_TRY(cudaMemcpyAsync(d->items, hp.items.data(), sizeof(int4) * hp.items.size(), cudaMemcpyHostToDevice,
+                                     c->stream));
+    if (!hp.hubs.empty())
+        DPG_CUDA_TRY(cudaMemcpyAsync(d->hubs, hp.hubs.data(), sizeof(int4) * hp.hubs.size(), cudaMemcpyHostToDevice,
+                                     c->stream));
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return DPG_OK;
+}
+
+dpg_status ensure_spmm_plan(dpg_graph* g) {
+    if (g->spmm_ready) return DPG_OK;
+    SpmmPlanHost hp;
+    build_spmm_plan(g->h_off.data(), g->V, &hp);
+    DPG_TRY(upload_spmm_plan(g->ctx, hp, &g->spmm_plan));
+    g->spmm_ready = true;
+    return DPG_OK;
+}
+
+dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
+                               const int32_t* weights, bool device_ptrs, dpg_graph** out);
+
+// Deterministic transposed CSR with the arc permutation: the columns come back to the host once,
+// dpg_csr_transpose_perm orders them as invertGraph does, and the result goes back up. With
+// need_graph the transposed CSR also becomes a graph of its own (g->tgraph).
+dpg_status ensure_spmm_transpose(dpg_graph* g, bool need_graph = false) {
+    if (g->spmm_t_ready && (!need_graph || g->tgraph)) return DPG_OK;
+    dpg_ctx* c = g->ctx;
+    const size_t nv = static_cast<size_t>(g->V), ne = static_cast<size_t>(g->E > 0 ? g->E : 1);
+    std::vector<int32_t> h_col(ne), t_off(nv + 1), t_col(ne), t_arc(ne);
+    if (g->E > 0) DPG_CUDA_TRY(cudaMemcpy(h_col.data(), g->col, static_cast<size_t>(g->E) * 4, cudaMemcpyDeviceToHost));
+    DPG_TRY(dpg_csr_transpose_perm(g->V, g->E, g->h_off.data(), h_col.data(), t_off.data(), t_col.data(), t_arc.data()));
+    if (!g->spmm_t_ready) {
+        DPG_CUDA_TRY(cudaMalloc(&g->tt_col, ne * 4));
+        DPG_CUDA_TRY(cudaMalloc(&g->tt_arc, ne * 4));
+        DPG_CUDA_TRY(cudaMemcpyAsync(g->tt_col, t_col.data(), ne * 4, cudaMemcpyHostToDevice, c->stream));
+        DPG_CUDA_TRY(cudaMemcpyAsync(g->tt_arc, t_arc.data(), ne * 4, cudaMemcpyHostToDevice, c->stream));
+        SpmmPlanHost hp;
+        build_spmm_plan(t_off.data(), g->V, &hp);
+        DPG_TRY(upload_spmm_plan(c, hp, &g->spmm_t_plan));
+        g->spmm_t_ready = true;
+    }
+    if (need_graph && !g->tgraph) {
+        DPG_TRY(graph_create_common(c, g->V, g->E, t_off.data(), t_col.data(), nullptr, false, &g->tgraph));
+        g->tgraph->relabel = g->relabel;
+    }
+    return DPG_OK;
+}
+
+dpg_status check_nrhs(int32_t nrhs) {
+    if (nrhs < 1 || nrhs > 128) return set_error(DPG_ERR_INVALID_ARG, "nrhs must be in [1, 128]");
+    return DPG_OK;
+}
 
 // Frontier queues, bitmaps and chunk lists from the context arena.
 dpg_status expand_workspace(dpg_ctx* c, int32_t V, int64_t E, int32_t min_chunked, ExpandWorkspace* wsp) {
@@ -667,6 +755,119 @@ dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* 
     return DPG_OK;
 }
 
+// Weighted PageRank to its fixed point, the adjoint fixed point for the seed dL/dr, and the per-arc
+// gradient (kernels and formulas in dpg_prgrad.cu). Sweeps stop when no entry changed by more than
+// the relative tolerance times its new value (forward: opts->epsilon on r; adjoint: adjoint_epsilon
+// on lambda), or after opts->iterations sweeps each; a tolerance <= 0 runs exactly that many.
+dpg_status run_pagerank_grad(dpg_ctx* c, dpg_graph* g, const float* d_w, const float* d_seed, const dpg_pr_opts* in_opts,
+                             double adjoint_epsilon, float* d_rank, float* d_grad) {
+    if (!g || g->ctx != c) return set_error(DPG_ERR_INVALID_ARG, "graph does not belong to this context");
+    dpg_pr_opts o;
+    DPG_TRY(pr_defaults(in_opts, &o));
+    if (g->V == 0) return DPG_OK;
+    if (!d_seed || !d_rank || (g->E > 0 && (!d_w || !d_grad)))
+        return set_error(DPG_ERR_INVALID_ARG, "null weights/seed/rank/grad");
+    // iterations == 0 with a tolerance means "until converged"; each loop still stops at kMaxGradSweeps.
+    constexpr int32_t kMaxGradSweeps = 10000;
+    const int32_t fwd_iters = std::min(o.iterations, kMaxGradSweeps);
+    int32_t adj_iters = fwd_iters;
+    if (adjoint_epsilon > 0 && (!in_opts || in_opts->iterations == 0)) adj_iters = kMaxGradSweeps;
+    DPG_TRY(ensure_spmm_transpose(g, true));
+    DPG_TRY(ensure_spmm_plan(g));
+    const size_t nv = static_cast<size_t>(g->V), ne = static_cast<size_t>(g->E > 0 ? g->E : 1);
+    const int nb = pr_vec_blocks(c->sm_count);
+    dpg_status st = DPG_OK;
+    float* w_t = static_cast<float*>(arena(c, S_VALS_T, ne * 4, &st));
+    float* W = static_cast<float*>(arena(c, S_PRG_W, nv * 4, &st));
+    float* y = static_cast<float*>(arena(c, S_PRG_Y, nv * 4, &st));
+    float* contrib = static_cast<float*>(arena(c, S_PRG_C, nv * 4, &st));
+    float* vec[4] = {static_cast<float*>(arena(c, S_PRG_V0, nv * 4, &st)),
+                     static_cast<float*>(arena(c, S_PRG_V1, nv * 4, &st)),
+                     static_cast<float*>(arena(c, S_PRG_V2, nv * 4, &st)),
+                     static_cast<float*>(arena(c, S_PRG_V3, nv * 4, &st))};
+    double* part = static_cast<double*>(arena(c, S_PRG_PART, static_cast<size_t>(nb) * 8, &st));
+    double* red = static_cast<double*>(arena(c, S_PRG_RED, 2 * 8, &st));
+    unsigned* flags = static_cast<unsigned*>(arena(c, S_PRG_FLAGS, 16, &st));  // [0] ticket, [1] nonstop
+    if (st != DPG_OK) return st;
+    DPG_CUDA_TRY(cudaMemsetAsync(flags, 0, 16, c->stream));
+    // Out-weight sums W = A 1 and the weights in transposed-slot order.
+    DPG_CUDA_TRY(launch_fill_f32(y, g->V, 1.0f, c->stream, c->sm_count));
+    DPG_TRY(run_spmv(c, g, d_w, y, W));
+    DPG_CUDA_TRY(launch_gather_values(d_w, g->tt_arc, g->E, w_t, c->stream, c->sm_count));
+
+    PrVecLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.V = g->V;
+    L.W = W;
+    L.part = part;
+    L.ticket = flags;
+    L.damping = static_cast<float>(o.damping);
+    auto sweeps_until = [&](int mode, int32_t cap, double eps, float** cur, float** nxt, dpg_graph* sg,
+                            const float* vals, const float* x_of_cur, int64_t* done) -> dpg_status {
+        // Every loop starts from the reduction its init pass left in red[0].
+        for (int32_t it = 0; it < cap; ++it) {
+            DPG_TRY(run_spmv(c, sg, vals, x_of_cur ? x_of_cur : *cur, y));
+            L.mode = mode;
+            L.y = y;
+            L.prev = eps > 0 ? *cur : nullptr;
+            L.out = *nxt;
+            L.red_in = red + (it & 1);
+            L.red_out = red + ((it + 1) & 1);
+            L.epsilon = static_cast<float>(eps);
+            L.nonstop = eps > 0 ? flags + 1 : nullptr;
+            if (eps > 0) DPG_CUDA_TRY(cudaMemsetAsync(flags + 1, 0, 4, c->stream));
+            DPG_CUDA_TRY(launch_pr_vec(L, c->sm_count, c->stream, &c->prof));
+            std::swap(*cur, *nxt);
+            ++*done;
+            if (eps > 0) {
+                unsigned h = 0;
+                DPG_CUDA_TRY(cudaMemcpyAsync(&h, flags + 1, 4, cudaMemcpyDeviceToHost, c->stream));
+                DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+                if (h == 0) break;
+            }
+        }
+        return DPG_OK;
+    };
+
+    // Forward: r in vec[0]/vec[1], contributions r / W in contrib, dangling sum in red[0].
+    float* r_cur = vec[0];
+    float* r_nxt = vec[1];
+    L.mode = PRV_FWD_INIT;
+    L.out = r_cur;
+    L.contrib = contrib;
+    L.init_value = o.init_zero ? 0.0f : static_cast<float>(o.total_rank / static_cast<double>(g->V));
+    L.red_out = red;
+    DPG_CUDA_TRY(launch_pr_vec(L, c->sm_count, c->stream, &c->prof));
+    L.base_const = (1.0 - o.damping) * o.total_rank / static_cast<double>(g->V);
+    L.red_scale = o.damping / static_cast<double>(g->V);
+    int64_t fwd = 0, adj = 0;
+    DPG_TRY(sweeps_until(PRV_FWD_SWEEP, fwd_iters, o.epsilon, &r_cur, &r_nxt, g->tgraph, w_t, contrib, &fwd));
+
+    // Adjoint: lambda in vec[2]/vec[3], its sum in red[0].
+    float* l_cur = vec[2];
+    float* l_nxt = vec[3];
+    L.mode = PRV_ADJ_INIT;
+    L.seed = d_seed;
+    L.out = l_cur;
+    L.prev = nullptr;
+    L.nonstop = nullptr;
+    L.red_out = red;
+    DPG_CUDA_TRY(launch_pr_vec(L, c->sm_count, c->stream, &c->prof));
+    L.base_const = 0.0;
+    L.red_scale = o.damping / static_cast<double>(g->V);
+    DPG_TRY(sweeps_until(PRV_ADJ_SWEEP, adj_iters, adjoint_epsilon, &l_cur, &l_nxt, g, d_w, nullptr, &adj));
+
+    // q = (A lambda) / W with the final lambda, then the per-arc gradient.
+    DPG_TRY(run_spmv(c, g, d_w, l_cur, y));
+    DPG_CUDA_TRY(launch_pr_arc_grad(g->spmm_plan, g->col, r_cur, W, y, l_cur, static_cast<float>(o.damping), d_grad,
+                                    c->stream, c->sm_count, &c->prof));
+    DPG_CUDA_TRY(cudaMemcpyAsync(d_rank, r_cur, nv * 4, cudaMemcpyDeviceToDevice, c->stream));
+    c->last_host_iterations = fwd + adj;
+    c->last_grad_sweeps[0] = fwd;
+    c->last_grad_sweeps[1] = adj;
+    return DPG_OK;
+}
+
 }  // namespace dpg_api
 
 extern "C" {
@@ -888,6 +1089,64 @@ dpg_status dpg_color(dpg_ctx* c, const dpg_graph* g, const dpg_expand_opts* opts
     DPG_TRY(run_color(c, const_cast<dpg_graph*>(g), opts, d));
     DPG_CUDA_TRY(cudaMemcpyAsync(h_color, d, static_cast<size_t>(g->V) * 4, cudaMemcpyDeviceToHost, c->stream));
     return check_device(c);
+}
+
+dpg_status dpg_spmm_f32_dev(dpg_ctx* c, const dpg_graph* gc, const float* d_vals, int32_t nrhs, const float* d_X,
+                            float* d_Y) {
+    DPG_TRY(use_device(c));
+    dpg_graph* g = const_cast<dpg_graph*>(gc);
+    if (!g || g->ctx != c) return set_error(DPG_ERR_INVALID_ARG, "graph does not belong to this context");
+    DPG_TRY(check_nrhs(nrhs));
+    if (g->V == 0) return DPG_OK;
+    if (!d_X || !d_Y || (g->E > 0 && !d_vals)) return set_error(DPG_ERR_INVALID_ARG, "null vals/X/Y");
+    DPG_TRY(ensure_spmm_plan(g));
+    dpg_status st = DPG_OK;
+    float* partial = static_cast<float*>(
+        arena(c, S_SPMM_PARTIAL, static_cast<size_t>(g->spmm_plan.nseg + 1) * nrhs * 4, &st));
+    if (st != DPG_OK) return st;
+    c->last_host_iterations = 1;
+    DPG_CUDA_TRY(launch_spmm(g->spmm_plan, g->col, d_vals, d_X, nrhs, d_Y, partial, c->stream, c->sm_count, &c->prof));
+    return DPG_OK;
+}
+
+dpg_status dpg_spmv_bwd_f32_dev(dpg_ctx* c, const dpg_graph* gc, const float* d_vals, int32_t nrhs, const float* d_X,
+                                const float* d_G, float* d_dX, float* d_dA) {
+    DPG_TRY(use_device(c));
+    dpg_graph* g = const_cast<dpg_graph*>(gc);
+    if (!g || g->ctx != c) return set_error(DPG_ERR_INVALID_ARG, "graph does not belong to this context");
+    DPG_TRY(check_nrhs(nrhs));
+    if (g->V == 0) return DPG_OK;
+    if (!d_G || (d_dA && !d_X) || (g->E > 0 && !d_vals)) return set_error(DPG_ERR_INVALID_ARG, "null vals/X/G");
+    c->last_host_iterations = 1;
+    if (d_dX) {
+        DPG_TRY(ensure_spmm_transpose(g));
+        dpg_status st = DPG_OK;
+        float* vals_t = static_cast<float*>(arena(c, S_VALS_T, static_cast<size_t>(g->E > 0 ? g->E : 1) * 4, &st));
+        float* partial = static_cast<float*>(
+            arena(c, S_SPMM_PARTIAL, static_cast<size_t>(g->spmm_t_plan.nseg + 1) * nrhs * 4, &st));
+        if (st != DPG_OK) return st;
+        DPG_CUDA_TRY(launch_gather_values(d_vals, g->tt_arc, g->E, vals_t, c->stream, c->sm_count));
+        DPG_CUDA_TRY(launch_spmm(g->spmm_t_plan, g->tt_col, vals_t, d_G, nrhs, d_dX, partial, c->stream, c->sm_count,
+                                 &c->prof));
+    }
+    if (d_dA) {
+        DPG_TRY(ensure_spmm_plan(g));
+        DPG_CUDA_TRY(launch_arc_dot(g->spmm_plan, g->col, d_X, d_G, nrhs, d_dA, c->stream, c->sm_count, &c->prof));
+    }
+    return DPG_OK;
+}
+
+dpg_status dpg_pagerank_grad_f32_dev(dpg_ctx* c, const dpg_graph* g, const float* d_weights, const float* d_seed,
+                                     const dpg_pr_opts* opts, double adjoint_epsilon, float* d_rank, float* d_grad) {
+    DPG_TRY(use_device(c));
+    return run_pagerank_grad(c, const_cast<dpg_graph*>(g), d_weights, d_seed, opts, adjoint_epsilon, d_rank, d_grad);
+}
+
+dpg_status dpg_ctx_grad_sweeps(const dpg_ctx* c, int64_t* forward, int64_t* adjoint) {
+    if (!c) return set_error(DPG_ERR_INVALID_ARG, "null context");
+    if (forward) *forward = c->last_grad_sweeps[0];
+    if (adjoint) *adjoint = c->last_grad_sweeps[1];
+    return DPG_OK;
 }
 
 dpg_status dpg_spmv_f32_dev(dpg_ctx* c, const dpg_graph* g, const float* d_vals, const float* d_x, float* d_y) {

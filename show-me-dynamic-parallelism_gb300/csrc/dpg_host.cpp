@@ -299,8 +299,8 @@ dpg_status dpg_csr_from_arcs(int32_t V, int64_t E, const int32_t* src, const int
     return DPG_OK;
 }
 
-dpg_status dpg_csr_transpose(int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
-                             int32_t* in_offsets, int32_t* in_col) {
+dpg_status dpg_csr_transpose_perm(int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
+                                  int32_t* in_offsets, int32_t* in_col, int32_t* in_arc) {
     if (V < 0 || E < 0 || E > INT32_MAX || !offsets || !in_offsets || (E > 0 && (!col || !in_col)))
         return set_error(DPG_ERR_INVALID_ARG, "dpg_csr_transpose: bad sizes or null pointers");
     if (offsets[0] != 0 || offsets[V] != E) return set_error(DPG_ERR_INVALID_ARG, "dpg_csr_transpose: offsets do not span E");
@@ -320,9 +320,18 @@ dpg_status dpg_csr_transpose(int32_t V, int64_t E, const int32_t* offsets, const
     // the back: the row of v lists its in-neighbours in the reverse of that push order.
     for (int32_t i = 0; i < V; ++i) {
         if (offsets[i + 1] < offsets[i]) return set_error(DPG_ERR_INVALID_ARG, "dpg_csr_transpose: offsets decrease");
-        for (int32_t j = offsets[i]; j < offsets[i + 1]; ++j) in_col[--cnt[col[j]]] = i;
+        for (int32_t j = offsets[i]; j < offsets[i + 1]; ++j) {
+            const int64_t pos = --cnt[col[j]];
+            in_col[pos] = i;
+            if (in_arc) in_arc[pos] = j;
+        }
     }
     return DPG_OK;
+}
+
+dpg_status dpg_csr_transpose(int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
+                             int32_t* in_offsets, int32_t* in_col) {
+    return dpg_csr_transpose_perm(V, E, offsets, col, in_offsets, in_col, nullptr);
 }
 
 dpg_status dpg_read_graph(const char* path, int32_t format, dpg_host_graph* out) {

@@ -140,6 +140,71 @@ struct RowGatherLaunch {
     unsigned* nonstop;      // nullable: set to 1 when some |new-old| > epsilon
 };
 
+// ---- batched right-hand sides / SpMV adjoint (dpg_adjoint.cu) -----------------------------------
+constexpr int kSpmmSegment = 512;  // nonzeros per item; longer rows are split and fixed up in order
+
+// Items {row, arc begin, arc end, segment index or -1}; hubs {row, first segment, segments, 0}.
+struct SpmmPlanHost {
+    std::vector<int4> items;
+    std::vector<int4> hubs;
+    int32_t nseg = 0;
+};
+struct SpmmPlanDev {
+    int4* items = nullptr;
+    int32_t nitems = 0;
+    int4* hubs = nullptr;
+    int32_t nhubs = 0;
+    int32_t nseg = 0;
+};
+void build_spmm_plan(const int32_t* off, int32_t V, SpmmPlanHost* plan);
+// Y[row][:] = sum over the row's arcs of val[e] * X[col[e]][:] (row-major [*][nrhs], nrhs <= 128);
+// partial holds nseg rows of nrhs.
+cudaError_t launch_spmm(const SpmmPlanDev& P, const int32_t* col, const float* val, const float* X, int nrhs, float* Y,
+                        float* partial, cudaStream_t s, int sm_count, LaunchHook* hook);
+// dA[e] = <G[row(e)][:], X[col[e]][:]>.
+cudaError_t launch_arc_dot(const SpmmPlanDev& P, const int32_t* col, const float* X, const float* G, int nrhs,
+                           float* dA, cudaStream_t s, int sm_count, LaunchHook* hook);
+// out[i] = v[idx[i]].
+cudaError_t launch_gather_values(const float* v, const int32_t* idx, int64_t n, float* out, cudaStream_t s,
+                                 int sm_count);
+
+// ---- weighted PageRank and its edge-weight gradient (dpg_prgrad.cu) ------------------------------
+
+enum PrVecMode {
+    PRV_FWD_INIT = 0,   // r = init_value; contrib = r / W; red_out = sum of r over dangling vertices
+    PRV_FWD_SWEEP = 1,  // r = (base_const + red_scale * red_in) + damping * y; contrib, red_out as above
+    PRV_ADJ_INIT = 2,   // lambda = seed; red_out = sum of lambda
+    PRV_ADJ_SWEEP = 3,  // lambda = seed + (W > 0 ? damping * y / W : red_scale * red_in); red_out = sum
+};
+
+struct PrVecLaunch {
+    int mode;
+    int32_t V;
+    const float* y;       // gathered sums of this sweep
+    const float* W;       // out-weight sums
+    const float* seed;    // dL/dr (adjoint)
+    const float* prev;    // previous vector for the change test, or null
+    float* out;           // new vector
+    float* contrib;       // forward: out / W, 0 where W == 0
+    const double* red_in; // reduction of the previous vector
+    double* red_out;
+    double* part;         // pr_vec_blocks(sm_count) partials
+    unsigned* ticket;     // zero before the first launch; the last block resets it
+    float damping;
+    float init_value;
+    double base_const;
+    double red_scale;
+    float epsilon;
+    unsigned* nonstop;    // set to 1 when some |out - prev| > epsilon * |out| (null: no test)
+};
+
+int pr_vec_blocks(int sm_count);
+cudaError_t launch_pr_vec(const PrVecLaunch& L, int sm_count, cudaStream_t s, LaunchHook* hook);
+cudaError_t launch_pr_arc_grad(const SpmmPlanDev& P, const int32_t* col, const float* r, const float* W, const float* y,
+                               const float* lam, float damping, float* grad, cudaStream_t s, int sm_count,
+                               LaunchHook* hook);
+cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s, int sm_count);
+
 // Column renaming by frequency (dpg_layout.cu).
 cudaError_t launch_column_histogram(const int32_t* col, int64_t E, int32_t* counts, cudaStream_t s, int sm_count);
 cudaError_t launch_relabel_columns(const int32_t* col, const int32_t* perm, int64_t E, int32_t* out, cudaStream_t s,
