@@ -47,9 +47,11 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["dpg", "reference"], default="dpg")
     ap.add_argument("--no-extra", action="store_true", help="skip the SpMV / SSSP / BFS side measurements")
-    ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs", "adjoint", "prgrad"], default="pagerank",
+    ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs", "adjoint", "prgrad", "batch"],
+                    default="pagerank",
                     help="pagerank is the headline; the others print their own line (used for profiling)")
     ap.add_argument("--scale", type=int, default=0, help="R-MAT scale for --workload spmv/sssp/bfs")
+    ap.add_argument("--batch-graphs", type=int, default=512, help="graphs in --workload batch")
     ap.add_argument("--no-relabel", action="store_true", help="turn off the column renaming of SpMV/PageRank")
     return ap.parse_args()
 
@@ -363,6 +365,108 @@ def measure_prgrad(dpg, ctx, torch, g, peak, reps=3):
             "grad_over_forward": t_all / t_fwd, "rank_sum": float(r.double().sum())}
 
 
+def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=512, reps=3):
+    """Batched workload: ngraphs seeded R-MAT graphs (V log-uniform in [1K, 1M], edge factor uniform
+    in {8, 16, 32}, weights uniform in [1, 100]), nsrc random SSSP sources and one sweeps-sweep
+    PageRank per graph. The batch (one CUDA-graph launch, autotuned) against looping the plain
+    single-graph kernels per source and per graph; results compared between the two."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t0 = time.perf_counter()
+    specs = dpg.rmat_batch_specs(ngraphs, seed=seed)
+    graphs = dpg.rmat_batch(specs, seed=seed * 1000)
+    t_gen = time.perf_counter() - t0
+    rng = np.random.default_rng(seed)
+    src = np.stack([rng.integers(0, g.V, nsrc) for g in graphs]).astype(np.int32)
+    t0 = time.perf_counter()
+    b = dpg.Batch(ctx, graphs)
+    t_pack = time.perf_counter() - t0
+    V, E = b.V, b.E
+    dist = torch.empty(nsrc * V, dtype=torch.int32, device=dev)
+    rank = torch.empty(V, dtype=torch.float32, device=dev)
+    t0 = time.perf_counter()
+    tuning = b.autotune(src)
+    t_tune = time.perf_counter() - t0
+    pr = {"iterations": sweeps, "damping": DAMPING, "total_rank": 1.0}
+    b.run(src, dist.data_ptr(), rank.data_ptr(), pr_opts_=pr)  # capture
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ts = []
+    for _ in range(reps):
+        e0.record()
+        b.run(src, dist.data_ptr(), rank.data_ptr(), pr_opts_=pr)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    ctx.synchronize()
+    t_batch = min(ts)
+    # Plain kernels, one call per graph and source (graphs resident before the timed loop).
+    plain = []
+    for g in graphs:
+        in_off, in_col = dpg.csr_transpose(g.V, g.offsets, g.col)
+        od = torch.from_numpy(np.diff(g.offsets).astype(np.int32)).to(dev)
+        plain.append((dpg.Graph(ctx, g.offsets, g.col, g.weights), dpg.Graph(ctx, in_off, in_col), od))
+    pdist = torch.empty(nsrc * V, dtype=torch.int32, device=dev)
+    prank = torch.empty(V, dtype=torch.float32, device=dev)
+
+    def loop():
+        for k, (go, gi, od) in enumerate(plain):
+            v0 = int(b.vstart[k])
+            for c in range(nsrc):
+                dpg.sssp_dev(ctx, go, int(src[k, c]), pdist[c * V + v0:].data_ptr())
+            dpg.pagerank_dev(ctx, gi, od.data_ptr(), prank[v0:].data_ptr(), damping=DAMPING, total_rank=1.0,
+                             iterations=sweeps)
+
+    loop()
+    ctx.synchronize()
+    tl = []
+    for _ in range(max(1, reps - 1)):
+        e0.record()
+        loop()
+        e1.record()
+        torch.cuda.synchronize()
+        tl.append(e0.elapsed_time(e1))
+    ctx.synchronize()
+    t_loop = min(tl)
+    # Split of both arms into their SSSP and PageRank parts (direct calls, not the captured graph).
+    def timed(fn):
+        fn()
+        ctx.synchronize()
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        return e0.elapsed_time(e1)
+
+    split = {
+        "ms_batch_sssp": timed(lambda: b.sssp_dev(src, dist.data_ptr())),
+        "ms_batch_pagerank": timed(lambda: b.pagerank_dev(rank.data_ptr(), **pr)),
+        "ms_loop_sssp": timed(lambda: [dpg.sssp_dev(ctx, go, int(src[k, c]), pdist[c * V + int(b.vstart[k]):].data_ptr())
+                                       for k, (go, _, _) in enumerate(plain) for c in range(nsrc)]),
+        "ms_loop_pagerank": timed(lambda: [dpg.pagerank_dev(ctx, gi, od.data_ptr(), prank[int(b.vstart[k]):].data_ptr(),
+                                                            damping=DAMPING, total_rank=1.0, iterations=sweeps)
+                                           for k, (_, gi, od) in enumerate(plain)]),
+    }
+    ctx.profile(True)
+    ctx.profile_reset()
+    b.sssp_dev(src, dist.data_ptr())
+    ctx.synchronize()
+    st = ctx.last_stats()
+    split["batch_sssp_iterations"] = int(st.iterations)
+    split["batch_sssp_arcs_scanned_over_E"] = st.edges_scanned / E
+    # The batch writes distances vertex-major (dist[v * nsrc + k]), the plain loop source-major.
+    sssp_equal = bool(torch.equal(dist.view(V, nsrc), pdist.view(nsrc, V).t()))
+    rmax = float(prank.max())
+    pr_err = float((rank - prank).abs().max()) / rmax
+    arcs = (nsrc + sweeps) * E
+    return {"graphs": ngraphs, "sources_per_graph": nsrc, "pagerank_sweeps": sweeps, "vertices": V, "arcs": E,
+            "ms_batch": t_batch, "ms_loop": t_loop, "speedup": t_loop / t_batch,
+            "gteps_batch": arcs / (t_batch / 1e3) / 1e9, "gteps_loop": arcs / (t_loop / 1e3) / 1e9,
+            "tuning": tuning, "kernels_per_batch": b.launches(), "plain_calls": ngraphs * (nsrc + 1),
+            "sssp_bit_exact_vs_plain": sssp_equal, "pagerank_max_err_over_max_rank": pr_err,
+            "s_generate": t_gen, "s_pack": t_pack, "s_autotune": t_tune, **split}
+
+
 def extra_measurements(dpg, ctx, torch, g, peak, steps):
     """SpMV on the scale-22 graph; SSSP and BFS on R-MAT scale 24 (device-resident, CUDA events)."""
     out = {"spmv_rmat22": measure_spmv(dpg, ctx, torch, g, peak, steps)}
@@ -387,7 +491,12 @@ def run_single_workload(args):
     peak, peak_kind = measured_peaks()
     ctx = dpg.Context(0)
     ctx.set_stream(stream.cuda_stream)
-    if args.workload == "prgrad":
+    if args.workload == "batch":
+        res = measure_batch(dpg, ctx, torch, peak, ngraphs=args.batch_graphs)
+        res["gteps"] = res["gteps_batch"]
+        scale = 0
+        g = None
+    elif args.workload == "prgrad":
         scale = args.scale or 20
         g = dpg.rmat_csr(scale, 16, seed=scale, weights=False)
         res = measure_prgrad(dpg, ctx, torch, g, peak)
@@ -404,9 +513,14 @@ def run_single_workload(args):
         scale = args.scale or 24
         g = dpg.rmat_csr(scale, 16, seed=scale, wmin=1, wmax=255)
         res = measure_expand(dpg, ctx, torch, g, peak, args.workload)
+    if g is None:
+        cfg = {"workload": f"batch of {res['graphs']} rmat graphs, V log-uniform [1K, 1M], edge factor "
+                           f"{{8, 16, 32}}, {res['sources_per_graph']} SSSP sources + {res['pagerank_sweeps']}-sweep "
+                           "PageRank each", "vertices": res["vertices"], "arcs": res["arcs"]}
+    else:
+        cfg = {"workload": f"{args.workload} rmat scale {scale} edge-factor 16", "vertices": g.V, "arcs": g.E}
     line = {"metric": f"GTEPS ({args.workload})", "value": res["gteps"], "unit": "GTEPS", "n_gpus": 1,
-            "config": {"workload": f"{args.workload} rmat scale {scale} edge-factor 16", "vertices": g.V,
-                       "arcs": g.E}, "peak_source": peak_kind, **res}
+            "config": cfg, "peak_source": peak_kind, **res}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -187,6 +187,43 @@ dpg_status dpg_pagerank_f32(dpg_ctx* ctx, const dpg_graph* g_in, const int32_t* 
 dpg_status dpg_pagerank_f32_dev(dpg_ctx* ctx, const dpg_graph* g_in, const int32_t* d_outdeg,
                                 const dpg_pr_opts* opts, float* d_rank);
 
+/* ---- batches of graphs (no counterpart in the reference) ---------------------------------------- */
+/* n graphs packed as one union CSR: graph g owns vertices [vstart[g], vstart[g+1]) and the union
+ * out-adjacency (offsets[V+1], col[E], weights[E], global vertex ids) keeps every arc inside its
+ * graph. The batch builds the union in-adjacency (invertGraph order per graph) for PageRank. */
+typedef struct dpg_batch dpg_batch;
+typedef struct dpg_batch_tuning {
+    int32_t hub_threshold; /* SSSP: out-degree from which a frontier vertex is cut into chunks (default 32) */
+    int32_t chunk;         /* SSSP: arcs per chunk, 128 / 256 / 512 (default 256) */
+    int32_t pr_hot;        /* PageRank: gathered entries kept in shared memory, -1 = as many as fit */
+} dpg_batch_tuning;
+dpg_status dpg_batch_create(dpg_ctx* ctx, int32_t ngraphs, const int32_t* vstart, int64_t E, const int32_t* offsets,
+                            const int32_t* col, const int32_t* weights, dpg_batch** out);
+dpg_status dpg_batch_destroy(dpg_batch* b);
+dpg_status dpg_batch_info(const dpg_batch* b, int32_t* ngraphs, int32_t* V, int64_t* E);
+dpg_status dpg_batch_set_tuning(dpg_batch* b, const dpg_batch_tuning* t);
+dpg_status dpg_batch_get_tuning(const dpg_batch* b, dpg_batch_tuning* t);
+/* SSSP from nsrc (1..32) sources of every graph in one persistent launch: h_sources[g * nsrc + k] is
+ * a vertex of graph g (local id); d_dist[v * nsrc + k] = distance of union vertex v from source k of
+ * v's graph (DPG_INF_COST when unreachable). Distances are exactly those of dpg_sssp on each graph
+ * alone. */
+dpg_status dpg_batch_sssp_dev(dpg_ctx* ctx, dpg_batch* b, int32_t nsrc, const int32_t* h_sources,
+                              const dpg_expand_opts* opts, int32_t* d_dist);
+/* opts->iterations sweeps of pull PageRank on every graph at once (opts->epsilon must be 0); each
+ * graph is normalised on its own (teleport and dangling mass over its V_g vertices), as dpg_pagerank
+ * on that graph alone with its out-degrees. d_rank[v] for union vertex v. */
+dpg_status dpg_batch_pagerank_dev(dpg_ctx* ctx, dpg_batch* b, const dpg_pr_opts* opts, float* d_rank);
+/* Both solves as one CUDA graph on the context stream: captured on the first call (and whenever an
+ * argument, the tuning or a scratch buffer changes), replayed on later calls. */
+dpg_status dpg_batch_run(dpg_ctx* ctx, dpg_batch* b, int32_t nsrc, const int32_t* h_sources,
+                         const dpg_expand_opts* sssp_opts, int32_t* d_dist, const dpg_pr_opts* pr_opts, float* d_rank);
+/* Kernel launches in one replay of the captured graph. */
+dpg_status dpg_batch_launches(const dpg_batch* b, int64_t* kernels_per_run);
+/* Times candidate tunings on this batch (SSSP binning on one source per graph; PageRank hot-cache
+ * size on three sweeps), keeps the fastest in the batch and returns it. Results never depend on it. */
+dpg_status dpg_batch_autotune(dpg_ctx* ctx, dpg_batch* b, int32_t nsrc, const int32_t* h_sources,
+                              dpg_batch_tuning* chosen);
+
 /* ---- one-shot host calls: the whole reference wrapper in one call (upload, solve, download) ---- */
 dpg_status dpg_sssp_host(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* offsets,
                          const int32_t* col, const int32_t* weights, int32_t source,

@@ -85,6 +85,13 @@ class PrOpts(ctypes.Structure):
     ]
 
 
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("hub_threshold", c_int32), ("chunk", c_int32), ("pr_hot", c_int32)]
+
+    def as_dict(self) -> dict:
+        return {"hub_threshold": self.hub_threshold, "chunk": self.chunk, "pr_hot": self.pr_hot}
+
+
 class RunStats(ctypes.Structure):
     _fields_ = [
         ("iterations", c_int64),
@@ -150,6 +157,16 @@ _SIGS = {
     "dpg_spmm_f32_dev": [_P, _P, _P, c_int32, _P, _P],
     "dpg_spmv_bwd_f32_dev": [_P, _P, _P, c_int32, _P, _P, _P, _P],
     "dpg_pagerank_grad_f32_dev": [_P, _P, _P, _P, _P, c_double, _P, _P],
+    "dpg_batch_create": [_P, c_int32, _P, c_int64, _P, _P, _P, _P],
+    "dpg_batch_destroy": [_P],
+    "dpg_batch_info": [_P, POINTER(c_int32), POINTER(c_int32), POINTER(c_int64)],
+    "dpg_batch_set_tuning": [_P, _P],
+    "dpg_batch_get_tuning": [_P, _P],
+    "dpg_batch_sssp_dev": [_P, _P, c_int32, _P, _P, _P],
+    "dpg_batch_pagerank_dev": [_P, _P, _P, _P],
+    "dpg_batch_run": [_P, _P, c_int32, _P, _P, _P, _P, _P],
+    "dpg_batch_launches": [_P, POINTER(c_int64)],
+    "dpg_batch_autotune": [_P, _P, c_int32, _P, _P],
     "dpg_ctx_grad_sweeps": [_P, POINTER(c_int64), POINTER(c_int64)],
     "dpg_write_dimacs9": [c_char_p, c_int32, c_int64, _P, _P, _P, c_int32],
     "dpg_write_cost": [c_char_p, c_int32, c_int32, _P],
@@ -434,6 +451,116 @@ class Graph:
             self.close()
         except Exception:
             pass
+
+
+class Batch:
+    """dpg_batch: many graphs packed as one union CSR on the context's device.
+
+    graphs: weighted CSRs (local vertex ids). vstart[g] is graph g's first union vertex."""
+
+    def __init__(self, ctx: Context, graphs):
+        self.ctx = ctx
+        self.n = len(graphs)
+        Vs = np.array([g.V for g in graphs], np.int64)
+        Es = np.array([g.E for g in graphs], np.int64)
+        self.vstart = np.zeros(self.n + 1, np.int64)
+        np.cumsum(Vs, out=self.vstart[1:])
+        estart = np.zeros(self.n + 1, np.int64)
+        np.cumsum(Es, out=estart[1:])
+        self.V, self.E = int(self.vstart[-1]), int(estart[-1])
+        if self.V >= 2**31 or self.E >= 2**31:
+            raise ValueError("a batch holds fewer than 2^31 vertices and arcs")
+        off = np.empty(self.V + 1, np.int32)
+        col = np.empty(max(self.E, 1), np.int32)
+        w = np.empty(max(self.E, 1), np.int32)
+        for k, g in enumerate(graphs):
+            v0, v1, e0, e1 = int(self.vstart[k]), int(self.vstart[k + 1]), int(estart[k]), int(estart[k + 1])
+            off[v0:v1] = np.asarray(g.offsets[:-1], np.int64) + e0
+            col[e0:e1] = np.asarray(g.col, np.int64) + v0
+            w[e0:e1] = g.weights
+        off[self.V] = self.E
+        self.vstart = self.vstart.astype(np.int32)
+        h = c_void_p()
+        _check(lib().dpg_batch_create(ctx.handle, self.n, _ptr(self.vstart), self.E, _ptr(off), _ptr(col), _ptr(w),
+                                      byref(h)))
+        self.handle = h
+
+    def sources_array(self, sources) -> np.ndarray:
+        src = _i32(sources)
+        if src.ndim != 2 or src.shape[0] != self.n:
+            raise ValueError("sources must be [ngraphs, nsrc]")
+        return np.ascontiguousarray(src)
+
+    def sssp_dev(self, sources, d_dist: int, **opts) -> None:
+        src = self.sources_array(sources)
+        o = expand_opts(**opts)
+        _check(lib().dpg_batch_sssp_dev(self.ctx.handle, self.handle, src.shape[1], _ptr(src), byref(o),
+                                        c_void_p(d_dist)))
+
+    def pagerank_dev(self, d_rank: int, **opts) -> None:
+        o = pr_opts(**opts)
+        _check(lib().dpg_batch_pagerank_dev(self.ctx.handle, self.handle, byref(o), c_void_p(d_rank)))
+
+    def run(self, sources, d_dist: int, d_rank: int, sssp_opts: dict | None = None,
+            pr_opts_: dict | None = None) -> None:
+        """Both solves as one CUDA-graph launch (captured on first use, replayed after)."""
+        src = self.sources_array(sources)
+        so = expand_opts(**(sssp_opts or {}))
+        po = pr_opts(**(pr_opts_ or {}))
+        _check(lib().dpg_batch_run(self.ctx.handle, self.handle, src.shape[1], _ptr(src), byref(so), c_void_p(d_dist),
+                                   byref(po), c_void_p(d_rank)))
+
+    def launches(self) -> int:
+        n = c_int64(0)
+        _check(lib().dpg_batch_launches(self.handle, byref(n)))
+        return int(n.value)
+
+    def autotune(self, sources) -> dict:
+        src = self.sources_array(sources)
+        t = BatchTuning()
+        _check(lib().dpg_batch_autotune(self.ctx.handle, self.handle, src.shape[1], _ptr(src), byref(t)))
+        return t.as_dict()
+
+    @property
+    def tuning(self) -> dict:
+        t = BatchTuning()
+        _check(lib().dpg_batch_get_tuning(self.handle, byref(t)))
+        return t.as_dict()
+
+    @tuning.setter
+    def tuning(self, d: dict) -> None:
+        t = BatchTuning(d["hub_threshold"], d["chunk"], d["pr_hot"])
+        _check(lib().dpg_batch_set_tuning(self.handle, byref(t)))
+
+    def close(self) -> None:
+        if self.handle:
+            lib().dpg_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def rmat_batch_specs(n: int, seed: int, vmin=1024, vmax=1 << 20, edge_factors=(8, 16, 32)):
+    """Vertex counts log-uniform in [vmin, vmax] and edge factors uniform over edge_factors."""
+    rng = np.random.default_rng(seed)
+    V = np.exp(rng.uniform(np.log(vmin), np.log(vmax), n)).astype(np.int64)
+    V = np.clip(V, vmin, vmax)
+    ef = rng.choice(np.asarray(edge_factors), n)
+    return [(int(v), int(e)) for v, e in zip(V, ef)]
+
+
+def rmat_batch(specs, seed: int, wmin=1, wmax=100):
+    """One seeded R-MAT(0.57,0.19,0.19,0.05) CSR per (V, edge factor); graph k uses seed + k."""
+    out = []
+    for k, (V, ef) in enumerate(specs):
+        scale = max(1, int(np.ceil(np.log2(V))))
+        src, dst, w = rmat_arcs(scale, V * ef, seed + k, wmin=wmin, wmax=wmax, V=V)
+        out.append(csr_from_arcs(V, src, dst, w))
+    return out
 
 
 def expand_opts(solution=SOL_BINNED, threshold=0, hub_threshold=0, max_iterations=0, timeout=0.0) -> ExpandOpts:

@@ -28,7 +28,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wextra", "-Wno-unused-parameter"]
 
-LIB_CU = ["dpg_api.cu", "dpg_expand.cu", "dpg_rowgather.cu", "dpg_noalloc.cu", "dpg_layout.cu", "dpg_adjoint.cu", "dpg_prgrad.cu"]
+LIB_CU = ["dpg_api.cu", "dpg_expand.cu", "dpg_rowgather.cu", "dpg_noalloc.cu", "dpg_layout.cu", "dpg_adjoint.cu", "dpg_prgrad.cu", "dpg_batch.cu"]
 LIB_CXX = ["dpg_host.cpp"]
 # app name -> source file (apps link against libdpg.so)
 APP_SOURCES = {

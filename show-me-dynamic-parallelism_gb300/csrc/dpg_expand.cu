@@ -51,21 +51,29 @@ struct ExpandParams {
     unsigned long long* trace;
     int32_t trace_cap;
     int32_t* aux;  // colouring: pending lower-neighbour count per vertex
+    // Multi-source SSSP (MaskSsspOp): label[v * nsrc + k] is v's distance from source k of v's
+    // graph; dirty[p][v] = (iteration tag << 32) | mask of the sources whose label of v changed.
+    int32_t nsrc;
+    unsigned long long* dirty[2];
 };
 
 // Operator interface of the expansion:
-//   row_value(u)           value carried with a popped vertex (its label, or its id)
-//   load_edge(e, rv)       neighbour v and candidate value of arc e
+//   RV                     type of the value carried with a popped vertex
+//   row_value(u)           that value (its label, or its id)
+//   load_edge(e, rv)       label index v, adjacency row r and candidate value of arc e's head
 //   want(v, cand, cur)     cheap filter before the atomic (cur = label[v] when kPeek)
 //   commit(v, cand)        the atomic update; true when v must be pushed
 struct SsspOp {
+    using RV = int;
     static constexpr bool kDedup = true;
     static constexpr bool kPeek = true;
-    __device__ __forceinline__ static int row_value(const ExpandParams& P, int u) { return __ldcg(P.label + u); }
-    __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v,
+    static constexpr bool kMask = false;
+    __device__ __forceinline__ static int row_value(const ExpandParams& P, int u, int) { return __ldcg(P.label + u); }
+    __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v, int& r,
                                                      int& cand) {
         const int2 a = __ldg(P.adj + e);
         v = a.x;
+        r = a.x;
         cand = du + a.y;
     }
     // Read-before-atomic filter (sssp_kernel.cu:55): labels only decrease, so a stale read can only
@@ -77,12 +85,15 @@ struct SsspOp {
 };
 
 struct BfsOp {
+    using RV = int;
     static constexpr bool kDedup = false;
     static constexpr bool kPeek = true;
-    __device__ __forceinline__ static int row_value(const ExpandParams& P, int u) { return __ldcg(P.label + u); }
-    __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v,
+    static constexpr bool kMask = false;
+    __device__ __forceinline__ static int row_value(const ExpandParams& P, int u, int) { return __ldcg(P.label + u); }
+    __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v, int& r,
                                                      int& cand) {
         v = __ldg(P.col + e);
+        r = v;
         cand = du + 1;
     }
     __device__ __forceinline__ static bool want(int, int, int cur) { return cur == DPG_UNDEFINED_LEVEL; }
@@ -95,11 +106,14 @@ struct BfsOp {
 // u < v. The expansion runs over the transposed graph: a coloured u decrements the pending count of
 // every in-neighbour v > u, and the decrement that reaches zero colours v and pushes it.
 struct ColorOp {
+    using RV = int;
     static constexpr bool kDedup = false;
     static constexpr bool kPeek = false;
-    __device__ __forceinline__ static int row_value(const ExpandParams&, int u) { return u; }
-    __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int u, int& v, int& cand) {
+    static constexpr bool kMask = false;
+    __device__ __forceinline__ static int row_value(const ExpandParams&, int u, int) { return u; }
+    __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int u, int& v, int& r, int& cand) {
         v = __ldg(P.col + e);
+        r = v;
         cand = u;
     }
     __device__ __forceinline__ static bool want(int v, int u, int) { return v > u; }
@@ -110,6 +124,46 @@ struct ColorOp {
     }
 };
 
+// SSSP from up to 32 sources per graph at once (a batch of graphs packed as one union CSR), in the
+// manner of multi-source traversal (Then et al., "The More the Merrier: Efficient Multi-Source
+// Graph Traversal", VLDB 2014): a frontier entry is a vertex with the mask of the sources whose
+// label of it changed, its labels label[v * nsrc + k] sit side by side, and one scan of its arcs
+// serves every source in the mask. The marks for the next frontier are 64-bit words
+// (iteration tag << 32 | mask) in a parity-indexed array: a tag other than the current iteration's
+// reads as an empty mask, so no clearing pass is needed.
+struct MaskSsspOp {
+    using RV = int2;  // {vertex, source mask}
+    static constexpr bool kDedup = false;
+    static constexpr bool kMask = true;
+    __device__ __forceinline__ static int2 row_value(const ExpandParams& P, int u, int j) {
+        const unsigned long long w = __ldcg(P.dirty[j & 1] + u);
+        const unsigned mask = (w >> 32) == static_cast<unsigned long long>(static_cast<unsigned>(j))
+                                  ? static_cast<unsigned>(w) : 0u;
+        return make_int2(u, static_cast<int>(mask));
+    }
+};
+
+// Adds `bits` to v's mark for the iteration `tag`; true when this call made the first mark of the
+// iteration (v must be pushed). A word changes at most nsrc + 1 times per iteration, so the loop
+// ends after at most that many failed compare-and-swaps.
+__device__ __forceinline__ bool tag_or(unsigned long long* w, unsigned tag, unsigned bits) {
+    const unsigned long long tg = static_cast<unsigned long long>(tag) << 32;
+    unsigned long long old = __ldcg(w);
+    for (;;) {
+        const bool fresh = (old >> 32) == static_cast<unsigned long long>(tag);
+        const unsigned long long want = fresh ? (old | bits) : (tg | bits);
+        if (want == old) return false;
+        const unsigned long long prev = atomicCAS(w, old, want);
+        if (prev == old) return !fresh;
+        old = prev;
+    }
+}
+
+__device__ __forceinline__ int shfl_rv(int v, int src) { return __shfl_sync(kFullMask, v, src); }
+__device__ __forceinline__ int2 shfl_rv(int2 v, int src) {
+    return make_int2(__shfl_sync(kFullMask, v.x, src), __shfl_sync(kFullMask, v.y, src));
+}
+
 // Destination buffers of one iteration's pushes.
 struct PushCtx {
     int32_t* qv;
@@ -118,6 +172,8 @@ struct PushCtx {
     uint32_t* bmp;
     int4* chunks;
     uint32_t* ccount;
+    unsigned long long* dirty;  // MaskSsspOp: marks of the next frontier
+    unsigned tag;               // MaskSsspOp: iteration of the next frontier
 };
 
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) {
@@ -127,9 +183,9 @@ __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) {
 // improved vertex v[u]. Vertices below the chunking degree go to the small queue with one
 // warp-aggregated append for all U slots; chunked vertices get their chunk range from one
 // warp-aggregated atomic per slot and the warp writes every chunk descriptor.
-template <class Op, bool kClassify, int U>
+template <class Op, bool kClassify, int CH, int U>
 __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx& Q, bool (&ok)[U],
-                                           const int (&v)[U]) {
+                                           const int (&v)[U], const int (&row)[U]) {
     bool any = false;
 #pragma unroll
     for (int u = 0; u < U; ++u) any |= ok[u];
@@ -147,8 +203,8 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
         s[u] = 0;
         e[u] = 0;
         if (ok[u]) {
-            s[u] = __ldg(P.off + v[u]);
-            e[u] = __ldg(P.off + v[u] + 1);
+            s[u] = __ldg(P.off + row[u]);
+            e[u] = __ldg(P.off + row[u] + 1);
         }
     }
     const int lane = lane_id();
@@ -186,7 +242,7 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
         for (int u = 0; u < U; ++u) {
             unsigned hm = __ballot_sync(kFullMask, chunked[u]);
             if (!hm) continue;
-            const int nch = chunked[u] ? (e[u] - s[u] + kHubChunk - 1) / kHubChunk : 0;
+            const int nch = chunked[u] ? (e[u] - s[u] + CH - 1) / CH : 0;
             const int incl = warp_inclusive_scan(nch);
             const int total = __shfl_sync(kFullMask, incl, 31);
             unsigned base = 0;
@@ -204,10 +260,10 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
                 const int hs = __shfl_sync(kFullMask, s[u], src);
                 const int he = __shfl_sync(kFullMask, e[u], src);
                 const unsigned first = __shfl_sync(kFullMask, my_first, src);
-                const int hn = (he - hs + kHubChunk - 1) / kHubChunk;
+                const int hn = (he - hs + CH - 1) / CH;
                 for (int c = lane; c < hn; c += 32) {
-                    const int k0 = hs + c * kHubChunk;
-                    __stcg(Q.chunks + first + c, make_int4(hv, k0, min(he, k0 + kHubChunk), c == 0 ? 1 : 0));
+                    const int k0 = hs + c * CH;
+                    __stcg(Q.chunks + first + c, make_int4(hv, k0, min(he, k0 + CH), c == 0 ? 1 : 0));
                 }
             }
         }
@@ -216,55 +272,92 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
 
 // U independent relaxations per lane, issued phase by phase (U adjacency loads, U label loads, U
 // atomics, one batched push) so each warp keeps U memory operations in flight instead of one.
-template <class Op, bool kClassify, int U>
+template <class Op, bool kClassify, int CH, int U>
 __device__ __forceinline__ void relax_batch(const ExpandParams& P, const PushCtx& Q, const bool (&act)[U],
-                                            const int (&e)[U], const int (&du)[U]) {
-    int v[U], cand[U], cur[U];
+                                            const int (&e)[U], const typename Op::RV (&du)[U]) {
+    int v[U], row[U];
     bool ok[U];
+    if constexpr (Op::kMask) {
+        // One adjacency read per arc; then, per source in the tail's mask, the reference's
+        // relaxation (sssp_kernel.cu:52-58) on that source's label of the head.
+        int w[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-        v[u] = 0;
-        cand[u] = 0;
-        if (act[u]) Op::load_edge(P, e[u], du[u], v[u], cand[u]);
+        for (int u = 0; u < U; ++u) {
+            v[u] = 0;
+            w[u] = 0;
+            if (act[u]) {
+                const int2 a = __ldg(P.adj + e[u]);
+                v[u] = a.x;
+                w[u] = a.y;
+            }
+            row[u] = v[u];
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            unsigned m = act[u] ? static_cast<unsigned>(du[u].y) : 0u;
+            const int32_t* lu = P.label + static_cast<int64_t>(du[u].x) * P.nsrc;
+            int32_t* lv = P.label + static_cast<int64_t>(v[u]) * P.nsrc;
+            unsigned bits = 0;
+            while (m) {
+                const int k = __ffs(m) - 1;
+                m &= m - 1u;
+                const int cand = __ldcg(lu + k) + w[u];
+                if (cand < __ldcg(lv + k) && cand < atomicMin(lv + k, cand)) bits |= 1u << k;
+            }
+            ok[u] = bits != 0u && tag_or(Q.dirty + v[u], Q.tag, bits);
+        }
+    } else {
+        int cand[U], cur[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            v[u] = 0;
+            row[u] = 0;
+            cand[u] = 0;
+            if (act[u]) Op::load_edge(P, e[u], du[u], v[u], row[u], cand[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) cur[u] = (Op::kPeek && act[u]) ? __ldcg(P.label + v[u]) : 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            ok[u] = act[u] && Op::want(v[u], cand[u], cur[u]) && Op::commit(P, v[u], cand[u]);
     }
-#pragma unroll
-    for (int u = 0; u < U; ++u) cur[u] = (Op::kPeek && act[u]) ? __ldcg(P.label + v[u]) : 0;
-#pragma unroll
-    for (int u = 0; u < U; ++u) ok[u] = act[u] && Op::want(v[u], cand[u], cur[u]) && Op::commit(P, v[u], cand[u]);
-    push_batch<Op, kClassify, U>(P, Q, ok, v);
+    push_batch<Op, kClassify, CH, U>(P, Q, ok, v, row);
 }
 
-template <class Op, bool kClassify>
+// Push of vertices whose label index is their row (single-source operators).
+template <class Op, bool kClassify, int CH>
 __device__ __forceinline__ void push_converged(const ExpandParams& P, const PushCtx& Q, bool ok, int v) {
     bool okb[1] = {ok};
     const int vb[1] = {v};
-    push_batch<Op, kClassify, 1>(P, Q, okb, vb);
+    push_batch<Op, kClassify, CH, 1>(P, Q, okb, vb, vb);
 }
 
 // Relaxation of one candidate per lane (all lanes call it together).
-template <class Op, bool kClassify>
-__device__ __forceinline__ void relax_one(const ExpandParams& P, const PushCtx& Q, bool act, int e, int du) {
+template <class Op, bool kClassify, int CH>
+__device__ __forceinline__ void relax_one(const ExpandParams& P, const PushCtx& Q, bool act, int e,
+                                          typename Op::RV du) {
     const bool a[1] = {act};
     const int ee[1] = {e};
-    const int dd[1] = {du};
-    relax_batch<Op, kClassify, 1>(P, Q, a, ee, dd);
+    const typename Op::RV dd[1] = {du};
+    relax_batch<Op, kClassify, CH, 1>(P, Q, a, ee, dd);
 }
 
 // Thread-per-vertex neighbour loops (the reference's serial loop), made warp-uniform so pushes can
 // aggregate over the full warp.
-template <class Op, bool kClassify>
+template <class Op, bool kClassify, int CH>
 __device__ __forceinline__ void serial_rows(const ExpandParams& P, const PushCtx& Q, bool act, int s,
-                                            int d, int du) {
+                                            int d, typename Op::RV du) {
     const int dd = act ? d : 0;
     const int wmax = __reduce_max_sync(kFullMask, dd);
-    for (int t = 0; t < wmax; ++t) relax_one<Op, kClassify>(P, Q, t < dd, s + t, du);
+    for (int t = 0; t < wmax; ++t) relax_one<Op, kClassify, CH>(P, Q, t < dd, s + t, du);
 }
 
 // Scan-based gather: the warp concatenates the rows of the active lanes and relaxes 32 consecutive
 // edges per step, so every step is a coalesced read whatever the per-row degrees are.
-template <class Op, bool kClassify>
+template <class Op, bool kClassify, int CH>
 __device__ __forceinline__ void warp_gather(const ExpandParams& P, const PushCtx& Q, bool act, int s,
-                                            int d, int du, int* sx, int* ss, int* sdu) {
+                                            int d, typename Op::RV du, int* sx, int* ss,
+                                            typename Op::RV* sdu) {
     const int lane = lane_id();
     const int dd = act ? d : 0;
     const int incl = warp_inclusive_scan(dd);
@@ -278,13 +371,14 @@ __device__ __forceinline__ void warp_gather(const ExpandParams& P, const PushCtx
     constexpr int U = 4;
     for (int base = 0; base < total; base += 32 * U) {
         bool act[U];
-        int ee[U], dd2[U];
+        int ee[U];
+        typename Op::RV dd2[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int k = base + 32 * u + lane;
             act[u] = k < total;
             ee[u] = 0;
-            dd2[u] = 0;
+            dd2[u] = typename Op::RV{};
             if (act[u]) {
                 int r = 0;
 #pragma unroll
@@ -294,19 +388,21 @@ __device__ __forceinline__ void warp_gather(const ExpandParams& P, const PushCtx
                 dd2[u] = sdu[r];
             }
         }
-        relax_batch<Op, kClassify, U>(P, Q, act, ee, dd2);
+        relax_batch<Op, kClassify, CH, U>(P, Q, act, ee, dd2);
     }
     __syncwarp();
 }
 
 // One vertex's row expanded by the whole warp (the per-vertex child of the naive variant).
-template <class Op, bool kClassify>
-__device__ __forceinline__ void warp_row(const ExpandParams& P, const PushCtx& Q, int s, int d, int du) {
+template <class Op, bool kClassify, int CH>
+__device__ __forceinline__ void warp_row(const ExpandParams& P, const PushCtx& Q, int s, int d,
+                                         typename Op::RV du) {
     const int lane = lane_id();
     constexpr int U = 4;
     for (int base = 0; base < d; base += 32 * U) {
         bool act[U];
-        int ee[U], dd[U];
+        int ee[U];
+        typename Op::RV dd[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int t = base + 32 * u + lane;
@@ -314,20 +410,21 @@ __device__ __forceinline__ void warp_row(const ExpandParams& P, const PushCtx& Q
             ee[u] = s + t;
             dd[u] = du;
         }
-        relax_batch<Op, kClassify, U>(P, Q, act, ee, dd);
+        relax_batch<Op, kClassify, CH, U>(P, Q, act, ee, dd);
     }
 }
 
-template <class Op, int POL>
+template <class Op, int POL, int CH = kHubChunk>
 __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
+    using RV = typename Op::RV;
     constexpr bool kClassify = (POL == DPG_SOL_GRID || POL == DPG_SOL_BINNED);
     __shared__ int s_excl[kWarps][32];
     __shared__ int s_start[kWarps][32];
-    __shared__ int s_du[kWarps][32];
+    __shared__ RV s_du[kWarps][32];
     // CTA consolidation buffer (DPG_SOL_BLOCK).
     __shared__ int c_start[kBlock];
     __shared__ int c_deg[kBlock];
-    __shared__ int c_du[kBlock];
+    __shared__ RV c_du[kBlock];
     __shared__ int c_excl[kBlock];
     __shared__ int c_wsum[kWarps];
     __shared__ int c_n;
@@ -366,7 +463,8 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
         // Parity selects are written as ternaries so the pointer pairs stay in registers.
         const PushCtx Q = {p ? P.ws.qv[0] : P.ws.qv[1], p ? P.ws.qse[0] : P.ws.qse[1],
                            P.ws.qcount + (j + 1) % 3, p ? P.ws.bmp[0] : P.ws.bmp[1],
-                           p ? P.ws.chunks[0] : P.ws.chunks[1], P.ws.ccount + (j + 1) % 3};
+                           p ? P.ws.chunks[0] : P.ws.chunks[1], P.ws.ccount + (j + 1) % 3,
+                           p ? P.dirty[0] : P.dirty[1], static_cast<unsigned>(j + 1)};
         const int32_t* qv_cur = p ? P.ws.qv[1] : P.ws.qv[0];
         const int2* qse_cur = p ? P.ws.qse[1] : P.ws.qse[0];
         uint32_t* bmp_cur = p ? P.ws.bmp[1] : P.ws.bmp[0];
@@ -379,20 +477,21 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
             for (unsigned r = 0; r < rounds; ++r) {
                 const unsigned chunk = r * per_round + blockIdx.x * kWarps + warp;
                 const unsigned i = chunk * 32u + lane;
-                int u = 0, s = 0, d = 0, du = 0;
+                int u = 0, s = 0, d = 0;
+                RV du{};
                 const bool has = chunk < fchunks && i < n;
                 if (has) {
                     u = __ldcg(qv_cur + i);
                     const int2 se = __ldcg(qse_cur + i);
                     s = se.x;
                     d = se.y - se.x;
-                    du = Op::row_value(P, u);
+                    du = Op::row_value(P, u, j);
                     if (Op::kDedup) __stcg(bmp_cur + (u >> 5), 0u);
                     my_pops += 1;
                     my_edges += static_cast<unsigned long long>(d);
                 }
                 const bool big = has && d >= P.threshold;
-                serial_rows<Op, false>(P, Q, has && !big, s, d, du);
+                serial_rows<Op, false, CH>(P, Q, has && !big, s, d, du);
                 if (big) {
                     const int slot = atomicAdd(&c_n, 1);
                     c_start[slot] = s;
@@ -419,7 +518,8 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                     const int total = c_total;
                     for (int base = 0; base < total; base += kBlock) {
                         const int k = base + static_cast<int>(threadIdx.x);
-                        int ee = 0, dd = 0;
+                        int ee = 0;
+                        RV dd{};
                         if (k < total) {
                             int rr = 0;
 #pragma unroll
@@ -428,7 +528,7 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                             ee = c_start[rr] + (k - c_excl[rr]);
                             dd = c_du[rr];
                         }
-                        relax_one<Op, false>(P, Q, k < total, ee, dd);
+                        relax_one<Op, false, CH>(P, Q, k < total, ee, dd);
                     }
                     __syncthreads();
                     if (threadIdx.x == 0) c_n = 0;
@@ -443,49 +543,51 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                     // Grid-wide consolidation: one chunk (<= 256 arcs) of a chunked vertex.
                     const int4 C = __ldcg(chunks_cur + item);
                     const int v0 = C.x, k0 = C.y, k1 = C.z;
-                    const int du = Op::row_value(P, v0);
+                    const RV du = Op::row_value(P, v0, j);
                     if (C.w && lane == 0) {
                         if (Op::kDedup) __stcg(bmp_cur + (v0 >> 5), 0u);
                         my_pops += 1;
                     }
                     if (lane == 0) my_edges += static_cast<unsigned long long>(k1 - k0);
                     {
-                        constexpr int U = kHubChunk / 32;  // the whole chunk in one batch
+                        constexpr int U = CH / 32;  // the whole chunk in one batch
                         bool act[U];
-                        int ee[U], dd[U];
+                        int ee[U];
+                        RV dd[U];
 #pragma unroll
                         for (int u = 0; u < U; ++u) {
                             ee[u] = k0 + 32 * u + lane;
                             act[u] = ee[u] < k1;
                             dd[u] = du;
                         }
-                        relax_batch<Op, kClassify, U>(P, Q, act, ee, dd);
+                        relax_batch<Op, kClassify, CH, U>(P, Q, act, ee, dd);
                     }
                     continue;
                 }
                 const unsigned chunk = item - hub_items;
                 const unsigned i = chunk * 32u + lane;
-                int u = 0, s = 0, d = 0, du = 0;
+                int u = 0, s = 0, d = 0;
+                RV du{};
                 const bool has = i < n;
                 if (has) {
                     u = __ldcg(qv_cur + i);
                     const int2 se = __ldcg(qse_cur + i);
                     s = se.x;
                     d = se.y - se.x;
-                    du = Op::row_value(P, u);
+                    du = Op::row_value(P, u, j);
                     if (Op::kDedup) __stcg(bmp_cur + (u >> 5), 0u);
                     my_pops += 1;
                     my_edges += static_cast<unsigned long long>(d);
                 }
                 if (POL == DPG_SOL_THREAD || POL == DPG_SOL_GRID) {
-                    serial_rows<Op, kClassify>(P, Q, has, s, d, du);
+                    serial_rows<Op, kClassify, CH>(P, Q, has, s, d, du);
                 } else if (POL == DPG_SOL_BINNED) {
-                    warp_gather<Op, kClassify>(P, Q, has, s, d, du, s_excl[warp], s_start[warp], s_du[warp]);
+                    warp_gather<Op, kClassify, CH>(P, Q, has, s, d, du, s_excl[warp], s_start[warp], s_du[warp]);
                 } else {
                     const bool big = has && d >= P.threshold;
-                    serial_rows<Op, kClassify>(P, Q, has && !big, s, d, du);
+                    serial_rows<Op, kClassify, CH>(P, Q, has && !big, s, d, du);
                     if (POL == DPG_SOL_WARP) {
-                        warp_gather<Op, kClassify>(P, Q, big, s, d, du, s_excl[warp], s_start[warp], s_du[warp]);
+                        warp_gather<Op, kClassify, CH>(P, Q, big, s, d, du, s_excl[warp], s_start[warp], s_du[warp]);
                     } else {  // DPG_SOL_NAIVE
                         unsigned bigmask = __ballot_sync(kFullMask, big);
                         while (bigmask) {
@@ -493,8 +595,8 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                             bigmask &= bigmask - 1u;
                             const int bs = __shfl_sync(kFullMask, s, src);
                             const int bd = __shfl_sync(kFullMask, d, src);
-                            const int bdu = __shfl_sync(kFullMask, du, src);
-                            warp_row<Op, kClassify>(P, Q, bs, bd, bdu);
+                            const RV bdu = shfl_rv(du, src);
+                            warp_row<Op, kClassify, CH>(P, Q, bs, bd, bdu);
                         }
                     }
                 }
@@ -556,6 +658,63 @@ __global__ void expand_init_kernel(ExpandParams P, int32_t source, int32_t init_
     }
 }
 
+// Multi-source start, part 1: every label to infinity, marks, bitmaps and counters cleared.
+__global__ void multi_fill_kernel(ExpandParams P, int64_t nlabels) {
+    const int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = tid; i < nlabels; i += stride) P.label[i] = DPG_INF_COST;
+    for (int64_t v = tid; v < P.V; v += stride) {
+        P.dirty[0][v] = 0ull;
+        P.dirty[1][v] = 0ull;
+    }
+    if (tid == 0) {
+        for (int k = 0; k < 3; ++k) {
+            P.ws.qcount[k] = 0u;
+            P.ws.ccount[k] = 0u;
+        }
+        P.st->bar_count = 0u;
+        P.st->iterations = 0ull;
+        P.st->edges = 0ull;
+        P.st->pops = 0ull;
+    }
+}
+
+// Part 2: sources[i] = v * nsrc + k (source k at vertex v) gets distance 0 and its bit in v's mark
+// for iteration 0; the first bit to arrive pushes v, cut into CH-arc chunks when its degree reaches
+// hub_threshold.
+template <int CH>
+__global__ void multi_seed_kernel(ExpandParams P, const int32_t* __restrict__ sources, int32_t nsources) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nsources; i += gridDim.x * blockDim.x) {
+        const int x = sources[i];
+        const int v = x / P.nsrc, k = x - v * P.nsrc;
+        P.label[x] = 0;
+        const unsigned long long old = atomicOr(P.dirty[0] + v, 1ull << k);  // tag 0 in the high word
+        if (old != 0ull) continue;
+        const int s = P.off[v], e = P.off[v + 1];
+        if (e <= s) continue;
+        if (e - s >= P.hub_threshold) {
+            const int nch = (e - s + CH - 1) / CH;
+            const unsigned first = atomicAdd(P.ws.ccount, static_cast<unsigned>(nch));
+            if (static_cast<int64_t>(first) + nch > P.ws.cap_chunks) {
+                raise_error(P.st, DPG_ERR_CAPACITY, 12);
+                continue;
+            }
+            for (int c = 0; c < nch; ++c) {
+                const int k0 = s + c * CH;
+                P.ws.chunks[0][first + c] = make_int4(v, k0, min(e, k0 + CH), c == 0 ? 1 : 0);
+            }
+        } else {
+            const unsigned pos = atomicAdd(P.ws.qcount, 1u);
+            if (static_cast<int64_t>(pos) >= P.ws.cap_v) {
+                raise_error(P.st, DPG_ERR_CAPACITY, 13);
+                continue;
+            }
+            P.ws.qv[0][pos] = v;
+            P.ws.qse[0][pos] = make_int2(s, e);
+        }
+    }
+}
+
 // Colouring start: pending[v] = out-neighbours u < v (with multiplicity); vertices with none take
 // colour 1 and form the first frontier over the transposed graph (P.off / P.col).
 __global__ void color_init_kernel(ExpandParams P, const int32_t* __restrict__ out_off,
@@ -563,7 +722,7 @@ __global__ void color_init_kernel(ExpandParams P, const int32_t* __restrict__ ou
     const int lane = lane_id();
     const int64_t wid = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    const PushCtx Q = {P.ws.qv[0], P.ws.qse[0], P.ws.qcount, P.ws.bmp[0], P.ws.chunks[0], P.ws.ccount};
+    const PushCtx Q = {P.ws.qv[0], P.ws.qse[0], P.ws.qcount, P.ws.bmp[0], P.ws.chunks[0], P.ws.ccount, nullptr, 0u};
     for (int64_t base = wid * 32; base < P.V; base += nw * 32) {  // warp-uniform trip count
         const int v = static_cast<int>(base) + lane;
         bool ready = false;
@@ -574,7 +733,7 @@ __global__ void color_init_kernel(ExpandParams P, const int32_t* __restrict__ ou
             P.label[v] = pending == 0 ? 1 : 0;
             ready = pending == 0;
         }
-        push_converged<ColorOp, true>(P, Q, ready, v < P.V ? v : 0);
+        push_converged<ColorOp, true, kHubChunk>(P, Q, ready, v < P.V ? v : 0);
     }
 }
 
@@ -600,11 +759,67 @@ const void* pick_kernel(int solution) {
 
 }  // namespace
 
-int64_t expand_chunk_capacity(int32_t V, int64_t E, int32_t min_chunked_degree) {
+int64_t expand_chunk_capacity(int32_t V, int64_t E, int32_t min_chunked_degree, int32_t chunk) {
     const int64_t d = min_chunked_degree < 1 ? 1 : min_chunked_degree;
     int64_t vertices = E / d + 1;
     if (vertices > static_cast<int64_t>(V) + 1) vertices = static_cast<int64_t>(V) + 1;
-    return E / kHubChunk + vertices + 1;
+    return E / (chunk < 1 ? kHubChunk : chunk) + vertices + 1;
+}
+
+namespace {
+template <int CH>
+cudaError_t run_multi(const MultiExpandLaunch& L, const ExpandWorkspace& ws, DevStatus* st, cudaStream_t stream,
+                      int sm_count, int* grid_out, LaunchHook* hook) {
+    const void* fn = reinterpret_cast<const void*>(expand_kernel<MaskSsspOp, DPG_SOL_BINNED, CH>);
+    int per_sm = 0;
+    cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlock, 0);
+    if (err != cudaSuccess) return err;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int grid = per_sm * sm_count;
+    ExpandParams P;
+    memset(&P, 0, sizeof(P));
+    P.off = L.off;
+    P.adj = L.adj;
+    P.label = L.label;
+    P.V = L.V;
+    P.threshold = L.hub_threshold;
+    P.hub_threshold = L.hub_threshold;
+    P.max_iter = L.max_iter;
+    P.timeout_ns = L.timeout_ns;
+    P.ws = ws;
+    P.st = st;
+    P.nsrc = L.nsrc;
+    P.dirty[0] = L.dirty[0];
+    P.dirty[1] = L.dirty[1];
+    const int64_t nlabels = static_cast<int64_t>(L.V) * L.nsrc;
+    {
+        HookScope hs(hook, DPG_KERNEL_INIT, stream);
+        multi_fill_kernel<<<sm_count * 8, kBlock, 0, stream>>>(P, nlabels);
+        if (L.nsources > 0)
+            multi_seed_kernel<CH><<<(L.nsources + kBlock - 1) / kBlock, kBlock, 0, stream>>>(P, L.sources, L.nsources);
+    }
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    void* args[] = {&P};
+    {
+        HookScope hs(hook, DPG_KERNEL_EXPAND, stream);
+        err = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kBlock), args, 0, stream);
+    }
+    if (grid_out) *grid_out = grid;
+    return err;
+}
+}  // namespace
+
+cudaError_t launch_expand_multi(const MultiExpandLaunch& L, const ExpandWorkspace& ws, DevStatus* st,
+                                cudaStream_t stream, int sm_count, int* grid_out, LaunchHook* hook) {
+    if (L.V < 1 || L.nsrc < 1 || L.nsrc > 32 || static_cast<int64_t>(L.V) * L.nsrc > INT32_MAX)
+        return cudaErrorInvalidValue;
+    switch (L.chunk) {
+        case 128: return run_multi<128>(L, ws, st, stream, sm_count, grid_out, hook);
+        case 256: return run_multi<256>(L, ws, st, stream, sm_count, grid_out, hook);
+        case 512: return run_multi<512>(L, ws, st, stream, sm_count, grid_out, hook);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_expand(const ExpandLaunch& L, const ExpandWorkspace& ws, DevStatus* st,

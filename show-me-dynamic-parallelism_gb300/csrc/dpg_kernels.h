@@ -69,11 +69,30 @@ struct ExpandLaunch {
 
 // Chunk capacity per parity for a graph of V vertices and E arcs when vertices of degree >=
 // min_chunked_degree are chunked: sum of ceil(deg/256) over distinct vertices of one iteration.
-int64_t expand_chunk_capacity(int32_t V, int64_t E, int32_t min_chunked_degree);
+int64_t expand_chunk_capacity(int32_t V, int64_t E, int32_t min_chunked_degree, int32_t chunk = kHubChunk);
 
 cudaError_t launch_expand(const ExpandLaunch& L, const ExpandWorkspace& ws, DevStatus* st,
                           cudaStream_t stream, int sm_count, int* grid_out, int* block_out,
                           LaunchHook* hook);
+
+// SSSP from nsrc <= 32 sources per graph at once over a union of graphs (label[v * nsrc + k]; the
+// marks dirty[2][V] are scratch); sources[i] = v * nsrc + k. Binned policy, chunk in {128, 256, 512}.
+struct MultiExpandLaunch {
+    const int32_t* off;
+    const int2* adj;
+    int32_t V;
+    int32_t nsrc;
+    int32_t* label;
+    unsigned long long* dirty[2];
+    const int32_t* sources;
+    int32_t nsources;
+    int32_t hub_threshold;
+    int32_t chunk;
+    int32_t max_iter;
+    unsigned long long timeout_ns;
+};
+cudaError_t launch_expand_multi(const MultiExpandLaunch& L, const ExpandWorkspace& ws, DevStatus* st,
+                                cudaStream_t stream, int sm_count, int* grid_out, LaunchHook* hook);
 
 // Greedy colouring over the transposed graph (L.off / L.col = in-CSR) with the persistent kernel;
 // out_off/out_col is the graph itself, pending a V-int scratch array, L.label the colours.
@@ -138,6 +157,12 @@ struct RowGatherLaunch {
     double* dfix;           // [fix-up warps] dangling partials
     float epsilon;
     unsigned* nonstop;      // nullable: set to 1 when some |new-old| > epsilon
+    // Batches of graphs (nullable): row v belongs to graph vgraph[v], whose uniform term this sweep
+    // is gbase[g] and whose initial rank is ginit[g]. A dangling row then stores its rank in its
+    // (never gathered) contribution slot, where the per-graph dangling reduction reads it.
+    const int32_t* vgraph;
+    const float* gbase;
+    const float* ginit;
 };
 
 // ---- batched right-hand sides / SpMV adjoint (dpg_adjoint.cu) -----------------------------------

@@ -58,12 +58,14 @@ __device__ __forceinline__ float load_product(const RowGatherLaunch& L, const fl
 // od / pos are the row's out-degree and contribution slot (perm[v] with renamed columns).
 __device__ __forceinline__ void pr_epilogue(const RowGatherLaunch& L, int v, float sum, float base, int od, int pos,
                                             double& dang) {
+    if (L.vgraph) base = __ldg(L.gbase + __ldg(L.vgraph + v));
     const float nv = fmaf(L.damping, sum, base);
     if (L.rank_out) L.rank_out[v] = nv;
     if (L.rank_prev && fabsf(nv - __ldg(L.rank_prev + v)) > L.epsilon) *L.nonstop = 1u;
-    // Only vertices with out-arcs are ever gathered (they are the columns), so dangling vertices
-    // write no contribution at all.
+    // Only vertices with out-arcs are ever gathered (they are the columns), so the contribution
+    // slot of a dangling vertex is free: a batch parks its rank there for the per-graph reduction.
     if (od > 0) L.y[pos] = nv / static_cast<float>(od);
+    else if (L.vgraph) L.y[pos] = nv;
     else dang += static_cast<double>(nv);
 }
 
@@ -261,9 +263,12 @@ __global__ void __launch_bounds__(kInitBlock) pr_init_kernel(RowGatherLaunch L, 
     double dang = 0.0;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < L.V; v += nthreads) {
         const int od = __ldg(L.outdeg + v);
-        if (od > 0) L.y[L.perm ? __ldg(L.perm + v) : v] = init_rank / static_cast<float>(od);
-        else dang += static_cast<double>(init_rank);
-        if (rank_prev) rank_prev[v] = init_rank;
+        const float r0 = L.vgraph ? __ldg(L.ginit + __ldg(L.vgraph + v)) : init_rank;
+        const int pos = L.perm ? __ldg(L.perm + v) : v;
+        if (od > 0) L.y[pos] = r0 / static_cast<float>(od);
+        else if (L.vgraph) L.y[pos] = r0;
+        else dang += static_cast<double>(r0);
+        if (rank_prev) rank_prev[v] = r0;
     }
     dang = warp_sum_f64(dang);
     if (lane == 0) L.dpart[gwarp] = dang;
