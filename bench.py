@@ -268,6 +268,7 @@ def measure_adjoint(dpg, ctx, torch, g, peak, nrhs=64, reps=5):
     """SpMV backward on g with lognormal(0,1) FP32 values and nrhs right-hand sides: the batched call
     (dX = A^T G and dA together) against looping the plain single-vector kernels once per column."""
     dev = torch.device("cuda", torch.cuda.current_device())
+    ctx.profile(False)  # no per-launch events in either arm
     V, E = g.V, g.E
     gen = torch.Generator(device=dev)
     gen.manual_seed(5)
@@ -371,6 +372,7 @@ def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=51
     PageRank per graph. The batch (one CUDA-graph launch, autotuned) against looping the plain
     single-graph kernels per source and per graph; results compared between the two."""
     dev = torch.device("cuda", torch.cuda.current_device())
+    ctx.profile(False)  # no per-launch events: they would slow the 4,608-call plain loop
     t0 = time.perf_counter()
     specs = dpg.rmat_batch_specs(ngraphs, seed=seed)
     graphs = dpg.rmat_batch(specs, seed=seed * 1000)
@@ -468,12 +470,18 @@ def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=51
 
 
 def extra_measurements(dpg, ctx, torch, g, peak, steps):
-    """SpMV on the scale-22 graph; SSSP and BFS on R-MAT scale 24 (device-resident, CUDA events)."""
+    """SpMV and the SpMV adjoint on the scale-22 graph; SSSP and BFS on R-MAT scale 24; the PageRank
+    edge-weight gradient on scale 20; the 512-graph batch (device-resident, CUDA events)."""
     out = {"spmv_rmat22": measure_spmv(dpg, ctx, torch, g, peak, steps)}
     out["spmv_bwd_rmat22_64rhs"] = measure_adjoint(dpg, ctx, torch, g, peak)
     g24 = dpg.rmat_csr(24, 16, seed=24, wmin=1, wmax=255)
     out["sssp_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "sssp")
     out["bfs_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "bfs")
+    del g24
+    g20 = dpg.rmat_csr(20, 16, seed=20, weights=False)
+    out["pagerank_grad_rmat20"] = measure_prgrad(dpg, ctx, torch, g20, peak)
+    del g20
+    out["batch_512_graphs"] = measure_batch(dpg, ctx, torch, peak)
     return out
 
 

@@ -90,11 +90,15 @@ dpg_status validate_offsets(const int32_t* off, int32_t V, int64_t E, int32_t* m
     if (off[0] != 0 || static_cast<int64_t>(off[V]) != E)
         return set_error(DPG_ERR_INVALID_ARG, "offsets must start at 0 and end at E");
     int32_t md = 0;
+    int64_t first_bad = INT64_MAX;
+#pragma omp parallel for reduction(max : md) reduction(min : first_bad) schedule(static)
     for (int32_t v = 0; v < V; ++v) {
         const int32_t d = off[v + 1] - off[v];
-        if (d < 0) return set_error(DPG_ERR_INVALID_ARG, "offsets decrease at vertex " + std::to_string(v));
+        if (d < 0 && v < first_bad) first_bad = v;
         if (d > md) md = d;
     }
+    if (first_bad != INT64_MAX)
+        return set_error(DPG_ERR_INVALID_ARG, "offsets decrease at vertex " + std::to_string(first_bad));
     *max_deg = md;
     return DPG_OK;
 }
@@ -191,45 +195,60 @@ int32_t hot_entries(const dpg_ctx* c, const dpg_graph* g) {
     return static_cast<int32_t>(cap < g->V ? cap : g->V);
 }
 
-// Builds perm/inv/pcol for the row gathers: column counts on the device, the frequency order on
-// the host (a 33-bucket stable multi-split), the renamed column array on the device. With
-// relabel_segments (vertex starts of packed graphs) each segment is ordered on its own, so renamed
-// ids stay inside their graph's range and each graph's gathers stay inside its own slice.
+// Builds perm/inv/pcol for the row gathers: column counts, the frequency order (a 33-class stable
+// multi-split) and the renamed column array, all on the device. With relabel_segments (vertex
+// starts of packed graphs) each segment is ordered on its own (on the host, once per batch), so
+// renamed ids stay inside their graph's range and each graph's gathers stay inside its own slice.
 dpg_status ensure_relabel(dpg_graph* g) {
     if (g->relabel_ready || g->V == 0) return DPG_OK;
     dpg_ctx* c = g->ctx;
     const size_t nv = static_cast<size_t>(g->V);
+    const std::vector<int32_t>& seg = g->relabel_segments;
     int32_t* counts = nullptr;
     DPG_CUDA_TRY(cudaMalloc(&counts, nv * 4));
-    std::vector<int32_t> h_counts(nv), h_perm(nv), h_inv(nv);
-    cudaError_t e = cudaMemsetAsync(counts, 0, nv * 4, c->stream);
+    cudaError_t e = cudaMalloc(&g->perm, nv * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&g->inv, nv * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&g->pcol, static_cast<size_t>(g->E > 0 ? g->E : 1) * 4);
+    if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, nv * 4, c->stream);
     if (e == cudaSuccess) e = launch_column_histogram(g->col, g->E, counts, c->stream, c->sm_count);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h_counts.data(), counts, nv * 4, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    cudaFree(counts);
-    if (e != cudaSuccess) return set_error(DPG_ERR_CUDA, std::string("column histogram: ") + cudaGetErrorString(e));
-    const std::vector<int32_t>& seg = g->relabel_segments;
-    if (seg.size() < 2) {
-        frequency_order(h_counts.data(), g->V, h_perm.data(), h_inv.data());
-    } else {
-        const int nseg = static_cast<int>(seg.size()) - 1;
+    if (e == cudaSuccess && seg.size() < 2) {
+        // One graph: the whole order on the device.
+        int32_t* scratch = nullptr;
+        e = cudaMalloc(&scratch, frequency_order_scratch_bytes(g->V));
+        if (e == cudaSuccess) e = launch_frequency_order(counts, g->V, scratch, g->perm, g->inv, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cudaFree(scratch);
+    } else if (e == cudaSuccess) {
+        // Packed graphs: each segment ordered on its own, on the host.
+        std::vector<int32_t> h_counts(nv), h_perm(nv), h_inv(nv);
+        e = cudaMemcpyAsync(h_counts.data(), counts, nv * 4, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e == cudaSuccess) {
+            const int nseg = static_cast<int>(seg.size()) - 1;
 #pragma omp parallel for schedule(dynamic, 1)
-        for (int k = 0; k < nseg; ++k) {
-            const int32_t lo = seg[k], n = seg[k + 1] - seg[k];
-            frequency_order(h_counts.data() + lo, n, h_perm.data() + lo, h_inv.data() + lo);
-            for (int32_t i = 0; i < n; ++i) {
-                h_perm[lo + i] += lo;
-                h_inv[lo + i] += lo;
+            for (int k = 0; k < nseg; ++k) {
+                const int32_t lo = seg[k], n = seg[k + 1] - seg[k];
+                frequency_order(h_counts.data() + lo, n, h_perm.data() + lo, h_inv.data() + lo);
+                for (int32_t i = 0; i < n; ++i) {
+                    h_perm[lo + i] += lo;
+                    h_inv[lo + i] += lo;
+                }
             }
+            e = cudaMemcpyAsync(g->perm, h_perm.data(), nv * 4, cudaMemcpyHostToDevice, c->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(g->inv, h_inv.data(), nv * 4, cudaMemcpyHostToDevice, c->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         }
     }
-    DPG_CUDA_TRY(cudaMalloc(&g->perm, nv * 4));
-    DPG_CUDA_TRY(cudaMalloc(&g->inv, nv * 4));
-    DPG_CUDA_TRY(cudaMalloc(&g->pcol, static_cast<size_t>(g->E > 0 ? g->E : 1) * 4));
-    DPG_CUDA_TRY(cudaMemcpyAsync(g->perm, h_perm.data(), nv * 4, cudaMemcpyHostToDevice, c->stream));
-    DPG_CUDA_TRY(cudaMemcpyAsync(g->inv, h_inv.data(), nv * 4, cudaMemcpyHostToDevice, c->stream));
-    DPG_CUDA_TRY(launch_relabel_columns(g->col, g->perm, g->E, g->pcol, c->stream, c->sm_count));
-    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    cudaFree(counts);
+    if (e == cudaSuccess) e = launch_relabel_columns(g->col, g->perm, g->E, g->pcol, c->stream, c->sm_count);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        cudaFree(g->perm);
+        cudaFree(g->inv);
+        cudaFree(g->pcol);
+        g->perm = g->inv = g->pcol = nullptr;
+        return set_error(DPG_ERR_CUDA, std::string("column renaming: ") + cudaGetErrorString(e));
+    }
     g->relabel_ready = true;
     return DPG_OK;
 }

@@ -242,6 +242,10 @@ cudaError_t launch_transpose_scatter(const int32_t* off, const int32_t* col, int
                                      int32_t* t_col, cudaStream_t s, int sm_count);
 // perm[old] = new, inv[new] = old; most frequent columns first (by bit length of the count), ties by id.
 void frequency_order(const int32_t* counts, int32_t V, int32_t* perm, int32_t* inv);
+// The same order computed on the device: scratch holds frequency_order_scratch_bytes(V).
+size_t frequency_order_scratch_bytes(int32_t V);
+cudaError_t launch_frequency_order(const int32_t* counts, int32_t V, int32_t* scratch, int32_t* perm, int32_t* inv,
+                                   cudaStream_t s);
 
 // Fills plan.lane_r0 from the tiles and the offsets (once per graph).
 cudaError_t launch_tile_lane_starts(const RowPlanDev& plan, const int32_t* off, cudaStream_t s, int sm_count);

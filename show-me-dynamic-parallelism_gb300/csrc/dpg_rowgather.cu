@@ -330,19 +330,19 @@ cudaError_t prepare_rowgather(size_t bytes) {
 
 }  // namespace
 
-void build_row_plan(const int32_t* off, int32_t V, RowPlanHost* plan) {
-    plan->tiles.clear();
-    plan->hubs_small.clear();
-    plan->hubs_big.clear();
-    plan->nseg = 0;
-    int32_t cur_row = 0, cur_rows = 0, cur_items = 0;
+namespace {
+// Greedy tiling of rows [r0, r1): consecutive rows share a tile while their merge items (rows +
+// nonzeros) fit in kRowTileItems; rows above kHubRowDegree become hubs cut into kRowTileItems
+// segments, numbered from 0 within this range.
+void plan_rows(const int32_t* off, int32_t r0, int32_t r1, RowPlanHost* plan) {
+    int32_t cur_row = r0, cur_rows = 0, cur_items = 0;
     auto flush = [&]() {
         if (cur_rows > 0)
             plan->tiles.push_back(make_int4(cur_row, cur_rows, off[cur_row], off[cur_row + cur_rows] - off[cur_row]));
         cur_rows = 0;
         cur_items = 0;
     };
-    for (int32_t r = 0; r < V; ++r) {
+    for (int32_t r = r0; r < r1; ++r) {
         const int32_t d = off[r + 1] - off[r];
         if (d > kHubRowDegree) {
             flush();
@@ -363,6 +363,32 @@ void build_row_plan(const int32_t* off, int32_t V, RowPlanHost* plan) {
         cur_items += d + 1;
     }
     flush();
+}
+}  // namespace
+
+// Rows are planned in fixed ranges of kPlanRange (independently, in parallel) and the ranges joined
+// with their hub segments renumbered, so the plan is the same whatever the thread count.
+void build_row_plan(const int32_t* off, int32_t V, RowPlanHost* plan) {
+    constexpr int32_t kPlanRange = 1 << 16;
+    const int32_t nr = V > 0 ? (V + kPlanRange - 1) / kPlanRange : 0;
+    std::vector<RowPlanHost> part(static_cast<size_t>(nr));
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int32_t k = 0; k < nr; ++k)
+        plan_rows(off, k * kPlanRange, std::min(V, (k + 1) * kPlanRange), &part[k]);
+    plan->tiles.clear();
+    plan->hubs_small.clear();
+    plan->hubs_big.clear();
+    plan->nseg = 0;
+    for (RowPlanHost& p : part) {
+        const int32_t base = plan->nseg;
+        for (int4 t : p.tiles) {
+            if (t.y < 0) t.y -= base;
+            plan->tiles.push_back(t);
+        }
+        for (int4 h : p.hubs_small) plan->hubs_small.push_back(make_int4(h.x, h.y + base, h.z, h.w));
+        for (int4 h : p.hubs_big) plan->hubs_big.push_back(make_int4(h.x, h.y + base, h.z, h.w));
+        plan->nseg += p.nseg;
+    }
 }
 
 cudaError_t launch_spmv(const RowGatherLaunch& L, DevStatus* st, cudaStream_t stream, int sm_count,
