@@ -366,39 +366,59 @@ def measure_prgrad(dpg, ctx, torch, g, peak, reps=3):
             "grad_over_forward": t_all / t_fwd, "rank_sum": float(r.double().sum())}
 
 
-def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=512, reps=3):
+def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=512, reps=3, rank=0, world=1):
     """Batched workload: ngraphs seeded R-MAT graphs (V log-uniform in [1K, 1M], edge factor uniform
     in {8, 16, 32}, weights uniform in [1, 100]), nsrc random SSSP sources and one sweeps-sweep
     PageRank per graph. The batch (one CUDA-graph launch, autotuned) against looping the plain
-    single-graph kernels per source and per graph; results compared between the two."""
+    single-graph kernels per source and per graph; results compared between the two.
+    Under torchrun the graphs are sharded over the ranks by LPT on arcs x tasks (no exchange);
+    times are the maximum over ranks."""
     dev = torch.device("cuda", torch.cuda.current_device())
     ctx.profile(False)  # no per-launch events: they would slow the 4,608-call plain loop
     t0 = time.perf_counter()
     specs = dpg.rmat_batch_specs(ngraphs, seed=seed)
-    graphs = dpg.rmat_batch(specs, seed=seed * 1000)
+    owner, load = dpg.partition_lpt([v * ef * (nsrc + sweeps) for v, ef in specs], world)
+    mine = [k for k in range(ngraphs) if owner[k] == rank]
+    graphs = [dpg.rmat_batch([specs[k]], seed=seed * 1000 + k)[0] for k in mine]
     t_gen = time.perf_counter() - t0
-    rng = np.random.default_rng(seed)
-    src = np.stack([rng.integers(0, g.V, nsrc) for g in graphs]).astype(np.int32)
+    src_all = np.random.default_rng(seed)
+    src_rows = [src_all.integers(0, v, nsrc) for v, _ in specs]
+    src = np.stack([src_rows[k] for k in mine]).astype(np.int32)
+    if world > 1:
+        import torch.distributed as tdist
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sync_all():
+        torch.cuda.synchronize()
+        if world > 1:
+            tdist.barrier()
     t0 = time.perf_counter()
     b = dpg.Batch(ctx, graphs)
     t_pack = time.perf_counter() - t0
     V, E = b.V, b.E
     dist = torch.empty(nsrc * V, dtype=torch.int32, device=dev)
-    rank = torch.empty(V, dtype=torch.float32, device=dev)
+    rank_v = torch.empty(V, dtype=torch.float32, device=dev)
     t0 = time.perf_counter()
     tuning = b.autotune(src)
     t_tune = time.perf_counter() - t0
     pr = {"iterations": sweeps, "damping": DAMPING, "total_rank": 1.0}
-    b.run(src, dist.data_ptr(), rank.data_ptr(), pr_opts_=pr)  # capture
+    b.run(src, dist.data_ptr(), rank_v.data_ptr(), pr_opts_=pr)  # capture
     ctx.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ts = []
     for _ in range(reps):
+        sync_all()
         e0.record()
-        b.run(src, dist.data_ptr(), rank.data_ptr(), pr_opts_=pr)
+        b.run(src, dist.data_ptr(), rank_v.data_ptr(), pr_opts_=pr)
         e1.record()
         torch.cuda.synchronize()
-        ts.append(e0.elapsed_time(e1))
+        ts.append(max_over_ranks(e0.elapsed_time(e1)))
     ctx.synchronize()
     t_batch = min(ts)
     # Plain kernels, one call per graph and source (graphs resident before the timed loop).
@@ -408,7 +428,7 @@ def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=51
         od = torch.from_numpy(np.diff(g.offsets).astype(np.int32)).to(dev)
         plain.append((dpg.Graph(ctx, g.offsets, g.col, g.weights), dpg.Graph(ctx, in_off, in_col), od))
     pdist = torch.empty(nsrc * V, dtype=torch.int32, device=dev)
-    prank = torch.empty(V, dtype=torch.float32, device=dev)
+    prank_v = torch.empty(V, dtype=torch.float32, device=dev)
 
     def loop():
         for k, (go, gi, od) in enumerate(plain):
@@ -422,11 +442,12 @@ def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=51
     ctx.synchronize()
     tl = []
     for _ in range(max(1, reps - 1)):
+        sync_all()
         e0.record()
         loop()
         e1.record()
         torch.cuda.synchronize()
-        tl.append(e0.elapsed_time(e1))
+        tl.append(max_over_ranks(e0.elapsed_time(e1)))
     ctx.synchronize()
     t_loop = min(tl)
     # Split of both arms into their SSSP and PageRank parts (direct calls, not the captured graph).
@@ -442,7 +463,7 @@ def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=51
 
     split = {
         "ms_batch_sssp": timed(lambda: b.sssp_dev(src, dist.data_ptr())),
-        "ms_batch_pagerank": timed(lambda: b.pagerank_dev(rank.data_ptr(), **pr)),
+        "ms_batch_pagerank": timed(lambda: b.pagerank_dev(rank_v.data_ptr(), **pr)),
         "ms_loop_sssp": timed(lambda: [dpg.sssp_dev(ctx, go, int(src[k, c]), pdist[c * V + int(b.vstart[k]):].data_ptr())
                                        for k, (go, _, _) in enumerate(plain) for c in range(nsrc)]),
         "ms_loop_pagerank": timed(lambda: [dpg.pagerank_dev(ctx, gi, od.data_ptr(), prank[int(b.vstart[k]):].data_ptr(),
@@ -459,12 +480,17 @@ def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=51
     # The batch writes distances vertex-major (dist[v * nsrc + k]), the plain loop source-major.
     sssp_equal = bool(torch.equal(dist.view(V, nsrc), pdist.view(nsrc, V).t()))
     rmax = float(prank.max())
-    pr_err = float((rank - prank).abs().max()) / rmax
+    pr_err = float((rank_v - prank).abs().max()) / rmax
     arcs = (nsrc + sweeps) * E
-    return {"graphs": ngraphs, "sources_per_graph": nsrc, "pagerank_sweeps": sweeps, "vertices": V, "arcs": E,
+    if world > 1:
+        t = torch.tensor([arcs], dtype=torch.float64, device=dev)
+        tdist.all_reduce(t)
+        arcs = float(t.item())
+    return {"ranks": world, "lpt_loads": [int(x) for x in load], "graphs_this_rank": len(mine), "graphs": ngraphs,
+            "sources_per_graph": nsrc, "pagerank_sweeps": sweeps, "vertices": V, "arcs": E,
             "ms_batch": t_batch, "ms_loop": t_loop, "speedup": t_loop / t_batch,
             "gteps_batch": arcs / (t_batch / 1e3) / 1e9, "gteps_loop": arcs / (t_loop / 1e3) / 1e9,
-            "tuning": tuning, "kernels_per_batch": b.launches(), "plain_calls": ngraphs * (nsrc + 1),
+            "tuning": tuning, "kernels_per_batch": b.launches(), "plain_calls": len(mine) * (nsrc + 1),
             "sssp_bit_exact_vs_plain": sssp_equal, "pagerank_max_err_over_max_rank": pr_err,
             "s_generate": t_gen, "s_pack": t_pack, "s_autotune": t_tune, **split}
 
@@ -485,23 +511,38 @@ def extra_measurements(dpg, ctx, torch, g, peak, steps):
     return out
 
 
-def run_single_workload(args):
-    """--workload spmv|sssp|bfs: one measurement, one JSON line (profiling entry point)."""
+def run_single_workload(args, world=1, rank=0, local=0):
+    """--workload spmv|sssp|bfs|adjoint|prgrad|batch: one measurement, one JSON line. Under torchrun
+    only the batch shards (LPT over ranks); the other workloads run on rank 0 alone."""
     import torch
 
     import __graft_entry__
 
     dpg = __graft_entry__.load_package()
-    dev = torch.device("cuda", 0)
+    if world > 1 and args.workload != "batch" and rank != 0:
+        return 0
+    dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    if world > 1 and args.workload == "batch":
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl", device_id=dev)
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
     peak, peak_kind = measured_peaks()
     ctx = dpg.Context(0)
     ctx.set_stream(stream.cuda_stream)
     if args.workload == "batch":
-        res = measure_batch(dpg, ctx, torch, peak, ngraphs=args.batch_graphs)
+        bw = world if world > 1 else 1
+        res = measure_batch(dpg, ctx, torch, peak, ngraphs=args.batch_graphs, rank=rank if bw > 1 else 0, world=bw)
         res["gteps"] = res["gteps_batch"]
+        if bw > 1:
+            import torch.distributed as tdist
+
+            tdist.barrier()
+            tdist.destroy_process_group()
+            if rank != 0:
+                return 0
         scale = 0
         g = None
     elif args.workload == "prgrad":
@@ -527,7 +568,8 @@ def run_single_workload(args):
                            "PageRank each", "vertices": res["vertices"], "arcs": res["arcs"]}
     else:
         cfg = {"workload": f"{args.workload} rmat scale {scale} edge-factor 16", "vertices": g.V, "arcs": g.E}
-    line = {"metric": f"GTEPS ({args.workload})", "value": res["gteps"], "unit": "GTEPS", "n_gpus": 1,
+    line = {"metric": f"GTEPS ({args.workload})", "value": res["gteps"], "unit": "GTEPS",
+            "n_gpus": world if args.workload == "batch" else 1,
             "config": cfg, "peak_source": peak_kind, **res}
     print(json.dumps(line), flush=True)
     return 0
@@ -663,7 +705,7 @@ def main() -> int:
     if args.impl == "reference":
         return run_reference(args, world, rank)
     if args.workload != "pagerank":
-        return run_single_workload(args)
+        return run_single_workload(args, world, rank, local)
     return run_dpg(args, world, rank, local)
 
 

@@ -224,6 +224,11 @@ dpg_status dpg_batch_launches(const dpg_batch* b, int64_t* kernels_per_run);
 dpg_status dpg_batch_autotune(dpg_ctx* ctx, dpg_batch* b, int32_t nsrc, const int32_t* h_sources,
                               dpg_batch_tuning* chosen);
 
+/* Shards a batch over `parts` ranks for the multi-GPU batched workload (no exchange step): owner[i]
+ * of unit i (a graph, with cost = arcs x tasks) by longest-processing-time-first; load[parts] gets
+ * each part's total cost (nullable). Deterministic: every rank computes the same owners. */
+dpg_status dpg_partition_lpt(int32_t n, const int64_t* cost, int32_t parts, int32_t* owner, int64_t* load);
+
 /* ---- one-shot host calls: the whole reference wrapper in one call (upload, solve, download) ---- */
 dpg_status dpg_sssp_host(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* offsets,
                          const int32_t* col, const int32_t* weights, int32_t source,

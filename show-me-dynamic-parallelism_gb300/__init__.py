@@ -167,6 +167,7 @@ _SIGS = {
     "dpg_batch_run": [_P, _P, c_int32, _P, _P, _P, _P, _P],
     "dpg_batch_launches": [_P, POINTER(c_int64)],
     "dpg_batch_autotune": [_P, _P, c_int32, _P, _P],
+    "dpg_partition_lpt": [c_int32, _P, c_int32, _P, _P],
     "dpg_ctx_grad_sweeps": [_P, POINTER(c_int64), POINTER(c_int64)],
     "dpg_write_dimacs9": [c_char_p, c_int32, c_int64, _P, _P, _P, c_int32],
     "dpg_write_cost": [c_char_p, c_int32, c_int32, _P],
@@ -542,6 +543,15 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def partition_lpt(costs, parts: int) -> tuple[np.ndarray, np.ndarray]:
+    """Owner rank of each unit (longest processing time first) and each rank's total cost."""
+    c = np.ascontiguousarray(costs, dtype=np.int64)
+    owner = np.empty(max(c.shape[0], 1), np.int32)
+    load = np.empty(parts, np.int64)
+    _check(lib().dpg_partition_lpt(int(c.shape[0]), _ptr(c), parts, _ptr(owner), _ptr(load)))
+    return owner[:c.shape[0]], load
 
 
 def rmat_batch_specs(n: int, seed: int, vmin=1024, vmax=1 << 20, edge_factors=(8, 16, 32)):

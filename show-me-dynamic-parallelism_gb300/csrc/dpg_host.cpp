@@ -13,6 +13,7 @@
 
 #include "dpg_internal.h"
 
+#include <algorithm>
 #include <cerrno>
 #include <cinttypes>
 #include <cmath>
@@ -508,6 +509,30 @@ dpg_status dpg_grid_arcs(int32_t rows, int32_t cols, uint64_t seed, int32_t wmin
             w[2 * k + 1] = wt;
         }
     }
+    return DPG_OK;
+}
+
+// Longest-processing-time-first: units by cost descending (ties: lower index first), each to the
+// part with the smallest load so far (ties: lower part). Deterministic, so every rank computes the
+// same owners on its own.
+dpg_status dpg_partition_lpt(int32_t n, const int64_t* cost, int32_t parts, int32_t* owner, int64_t* load) {
+    if (n < 0 || parts < 1 || (n > 0 && (!cost || !owner)))
+        return set_error(DPG_ERR_INVALID_ARG, "need n >= 0, parts >= 1, costs and owners");
+    for (int32_t i = 0; i < n; ++i)
+        if (cost[i] < 0) return set_error(DPG_ERR_INVALID_ARG, "costs must be >= 0");
+    std::vector<int32_t> order(static_cast<size_t>(n));
+    for (int32_t i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });
+    std::vector<int64_t> ld(static_cast<size_t>(parts), 0);
+    for (int32_t i : order) {
+        int32_t best = 0;
+        for (int32_t p = 1; p < parts; ++p)
+            if (ld[p] < ld[best]) best = p;
+        owner[i] = best;
+        ld[best] += cost[i];
+    }
+    if (load)
+        for (int32_t p = 0; p < parts; ++p) load[p] = ld[p];
     return DPG_OK;
 }
 
