@@ -26,6 +26,8 @@ BIN = PKG / "bin"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", "--expt-relaxed-constexpr"]
+# Extra nvcc flags for tuning builds, e.g. DPG_NVCC_EXTRA="-DDPG_GATHER_TILES=1" (use with --force).
+NVCC_FLAGS += os.environ.get("DPG_NVCC_EXTRA", "").split()
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wextra", "-Wno-unused-parameter"]
 
 LIB_CU = ["dpg_api.cu", "dpg_expand.cu", "dpg_rowgather.cu", "dpg_noalloc.cu", "dpg_layout.cu", "dpg_adjoint.cu", "dpg_prgrad.cu", "dpg_batch.cu"]

@@ -35,6 +35,15 @@ constexpr int kWarps = kBlock / 32;
 constexpr int kInitBlock = 256;
 constexpr int kIpl = kRowTileItems / 32;  // merge items per lane
 constexpr int kFixBlock = 256;
+// Tiles a warp carries through one step (see rowgather_kernel), per mode. Measured on R-MAT scale
+// 22 with the next step's descriptors prefetched: PageRank runs best with 1 (0.29 ms per sweep;
+// at 3 its registers spill), SpMV with 2 (145.5 GTEPS against 139.8 with 3, which spills).
+#ifndef DPG_GATHER_TILES_SPMV
+#define DPG_GATHER_TILES_SPMV 2
+#endif
+#ifndef DPG_GATHER_TILES_PR
+#define DPG_GATHER_TILES_PR 1
+#endif
 // Shared-memory index with one pad word per 32: lane l walking items 8l.. then hits 32 distinct banks
 // instead of 4 (an 8-way conflict without the pad).
 constexpr int kPadded = kRowTileItems + kRowTileItems / 32;
@@ -77,7 +86,10 @@ __device__ __forceinline__ float pr_base(const RowGatherLaunch& L) {
     return static_cast<float>(L.base_const + L.dangling_scale * __ldg(L.dsum_in));
 }
 
-template <int MODE>
+// One step of a warp covers KT consecutive tiles: first every column, row-end and epilogue load of
+// all KT tiles, then all their gathers, then the tiles are walked one after the other through the
+// warp's single staging area. A lane thus keeps KT x 8 gathers in flight instead of 8.
+template <int MODE, int KT>
 __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
     extern __shared__ __align__(16) unsigned char rg_smem[];
     const int warp = threadIdx.x >> 5;
@@ -94,105 +106,134 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
     if (MODE == kModePagerank) base = pr_base(L);
     double dang = 0.0;
 
-    // Each warp walks its tiles with the next descriptor and lane starts already in flight.
     const int ntiles = L.plan.ntiles;
-    int t = gwarp;
-    int4 T = t < ntiles ? __ldg(L.plan.tiles + t) : make_int4(0, 0, 0, 0);
-    int r0 = t < ntiles ? __ldg(L.plan.lane_r0 + t * 32 + lane) : 0;
-    for (; t < ntiles; t += nwarps) {
-        const int tn = t + nwarps;
-        const int4 Tn = tn < ntiles ? __ldg(L.plan.tiles + tn) : make_int4(0, 0, 0, 0);
-        const int r0n = tn < ntiles ? __ldg(L.plan.lane_r0 + tn * 32 + lane) : 0;
-        const int row = T.x, nrows = T.y, nb = T.z, nnz = T.w;
-        if (nrows < 0) {
-            // Hub segment: fixed-order lane sums, then a butterfly; partial goes to the fix-up.
-            float acc = 0.0f;
+    // Descriptors and lane starts of the next step are requested one step ahead.
+    int4 Tn[KT];
+    int r0n[KT];
+#pragma unroll
+    for (int k = 0; k < KT; ++k) {
+        const int t = gwarp * KT + k;
+        Tn[k] = t < ntiles ? __ldg(L.plan.tiles + t) : make_int4(0, 0, 0, 0);
+        r0n[k] = t < ntiles ? __ldg(L.plan.lane_r0 + t * 32 + lane) : 0;
+    }
+    for (int t0 = gwarp * KT; t0 < ntiles; t0 += nwarps * KT) {
+        int4 T[KT];
+        int r0[KT], re0[KT], od0[KT], pos0[KT];
+        float pv[KT][kIpl];
+        // Phase 1: columns, the first 32 row ends and epilogue inputs of every tile.
+        int cols[KT][kIpl];
+#pragma unroll
+        for (int k = 0; k < KT; ++k) {
+            T[k] = Tn[k];
+            r0[k] = r0n[k];
+            const int row = T[k].x, nrows = T[k].y, nb = T[k].z, nnz = T[k].w;
 #pragma unroll
             for (int i = 0; i < kIpl; ++i) {
                 const int j = i * 32 + lane;
-                if (j < nnz) acc += load_product<MODE>(L, s_hot, nb + j);
+                cols[k][i] = j < nnz ? __ldg(L.col + nb + j) : 0;
             }
-            acc = warp_sum_f32(acc);
-            if (lane == 0) L.partial[-(nrows + 1)] = acc;
-            T = Tn;
-            r0 = r0n;
-            continue;
-        }
-        // Epilogue inputs of the first 32 rows, requested before the gathers.
-        int od0 = 0, pos0 = 0;
-        if (MODE == kModePagerank && lane < nrows) {
-            od0 = __ldg(L.outdeg + row + lane);
-            pos0 = L.perm ? __ldg(L.perm + row + lane) : row + lane;
-        }
-        // Stage relative row ends and products.
-        for (int r = lane; r < nrows; r += 32) re[pad(r)] = __ldg(L.off + row + r + 1) - nb;
-        int cols[kIpl];
-#pragma unroll
-        for (int i = 0; i < kIpl; ++i) {
-            const int j = i * 32 + lane;
-            cols[i] = j < nnz ? __ldg(L.col + nb + j) : 0;
-        }
-#pragma unroll
-        for (int i = 0; i < kIpl; ++i) {
-            const int j = i * 32 + lane;
-            if (j < nnz) {
-                float pv = gather_x(L, s_hot, cols[i]);
-                if (MODE == kModeSpmv) pv *= __ldg(L.vals + nb + j);
-                val[pad(j)] = pv;
+            re0[k] = lane < nrows ? __ldg(L.off + row + lane + 1) - nb : 0;
+            od0[k] = 0;
+            pos0[k] = 0;
+            if (MODE == kModePagerank && lane < nrows) {
+                od0[k] = __ldg(L.outdeg + row + lane);
+                pos0[k] = L.perm ? __ldg(L.perm + row + lane) : row + lane;
             }
         }
-        __syncwarp();
-        // Merge-path: lane owns merge items [d0, d1) starting at row r0 (precomputed per tile);
-        // r = row ends consumed, k = nonzeros consumed. The walk is branch-free.
-        const int total = nrows + nnz;
-        const int d0 = min(lane * kIpl, total);
-        const int d1 = min(d0 + kIpl, total);
-        int r = d0 < total ? r0 : nrows;
-        int k = d0 - r;
-        float acc = 0.0f;
-        int first_emit = -1;
-        int rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
 #pragma unroll
-        for (int i = 0; i < kIpl; ++i) {
-            const bool live = d0 + i < d1;
-            const bool take = live && k < rend;
-            const bool emit = live && !(k < rend);
-            const float v = val[pad(k)];  // k <= nnz <= 255 stays inside the padded row
-            if (emit) {
-                out[pad(r)] = acc;
-                first_emit = first_emit < 0 ? r : first_emit;
-            }
-            acc = take ? acc + v : (emit ? 0.0f : acc);
-            k += take ? 1 : 0;
-            r += emit ? 1 : 0;
-            if (emit) rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
+        for (int k = 0; k < KT; ++k) {
+            const int t = t0 + nwarps * KT + k;
+            Tn[k] = t < ntiles ? __ldg(L.plan.tiles + t) : make_int4(0, 0, 0, 0);
+            r0n[k] = t < ntiles ? __ldg(L.plan.lane_r0 + t * 32 + lane) : 0;
         }
-        // Segmented inclusive scan of the lanes' open partials (key = row still open at lane end).
-        float cv = acc;
-        const int key = r;
+        // Phase 2: the gathers of every tile.
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const float tv = __shfl_up_sync(kFullMask, cv, o);
-            const int tk = __shfl_up_sync(kFullMask, key, o);
-            if (lane >= o && tk == key) cv += tv;
-        }
-        const float cin = __shfl_up_sync(kFullMask, cv, 1);
-        const int kin = __shfl_up_sync(kFullMask, key, 1);
-        if (lane > 0 && first_emit >= 0 && kin == first_emit) out[pad(first_emit)] += cin;
-        __syncwarp();
-        for (int rr = lane; rr < nrows; rr += 32) {
-            const float sum = out[pad(rr)];
-            if (MODE == kModeSpmv) {
-                L.y[row + rr] = sum;
-            } else if (rr < 32) {
-                pr_epilogue(L, row + rr, sum, base, od0, pos0, dang);
-            } else {
-                pr_epilogue(L, row + rr, sum, base, dang);
+        for (int k = 0; k < KT; ++k) {
+            const int nb = T[k].z, nnz = T[k].w;
+#pragma unroll
+            for (int i = 0; i < kIpl; ++i) {
+                const int j = i * 32 + lane;
+                float v = 0.0f;
+                if (j < nnz) {
+                    v = gather_x(L, s_hot, cols[k][i]);
+                    if (MODE == kModeSpmv) v *= __ldg(L.vals + nb + j);
+                }
+                pv[k][i] = v;
             }
         }
-        __syncwarp();
-        T = Tn;
-        r0 = r0n;
+        // Phase 3: each tile through the staging area.
+#pragma unroll
+        for (int k = 0; k < KT; ++k) {
+            if (t0 + k >= ntiles) break;
+            const int row = T[k].x, nrows = T[k].y, nb = T[k].z, nnz = T[k].w;
+            if (nrows < 0) {
+                // Hub segment: fixed-order lane sums, then a butterfly; partial goes to the fix-up.
+                float acc = 0.0f;
+#pragma unroll
+                for (int i = 0; i < kIpl; ++i)
+                    if (i * 32 + lane < nnz) acc += pv[k][i];
+                acc = warp_sum_f32(acc);
+                if (lane == 0) L.partial[-(nrows + 1)] = acc;
+                continue;
+            }
+            if (lane < nrows) re[pad(lane)] = re0[k];
+            for (int r = lane + 32; r < nrows; r += 32) re[pad(r)] = __ldg(L.off + row + r + 1) - nb;
+#pragma unroll
+            for (int i = 0; i < kIpl; ++i) {
+                const int j = i * 32 + lane;
+                if (j < nnz) val[pad(j)] = pv[k][i];
+            }
+            __syncwarp();
+            // Merge-path: lane owns merge items [d0, d1) starting at row r0 (precomputed per tile);
+            // r = row ends consumed, kk = nonzeros consumed. The walk is branch-free.
+            const int total = nrows + nnz;
+            const int d0 = min(lane * kIpl, total);
+            const int d1 = min(d0 + kIpl, total);
+            int r = d0 < total ? r0[k] : nrows;
+            int kk = d0 - r;
+            float acc = 0.0f;
+            int first_emit = -1;
+            int rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
+#pragma unroll
+            for (int i = 0; i < kIpl; ++i) {
+                const bool live = d0 + i < d1;
+                const bool take = live && kk < rend;
+                const bool emit = live && !(kk < rend);
+                const float v = val[pad(kk)];  // kk <= nnz <= 255 stays inside the padded row
+                if (emit) {
+                    out[pad(r)] = acc;
+                    first_emit = first_emit < 0 ? r : first_emit;
+                }
+                acc = take ? acc + v : (emit ? 0.0f : acc);
+                kk += take ? 1 : 0;
+                r += emit ? 1 : 0;
+                if (emit) rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
+            }
+            // Segmented inclusive scan of the lanes' open partials (key = row still open at lane end).
+            float cv = acc;
+            const int key = r;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const float tv = __shfl_up_sync(kFullMask, cv, o);
+                const int tk = __shfl_up_sync(kFullMask, key, o);
+                if (lane >= o && tk == key) cv += tv;
+            }
+            const float cin = __shfl_up_sync(kFullMask, cv, 1);
+            const int kin = __shfl_up_sync(kFullMask, key, 1);
+            if (lane > 0 && first_emit >= 0 && kin == first_emit) out[pad(first_emit)] += cin;
+            __syncwarp();
+            for (int rr = lane; rr < nrows; rr += 32) {
+                const float sum = out[pad(rr)];
+                if (MODE == kModeSpmv) {
+                    L.y[row + rr] = sum;
+                } else if (rr < 32) {
+                    pr_epilogue(L, row + rr, sum, base, od0[k], pos0[k], dang);
+                } else {
+                    pr_epilogue(L, row + rr, sum, base, dang);
+                }
+            }
+            __syncwarp();
+        }
     }
     if (MODE == kModePagerank) {
         dang = warp_sum_f64(dang);
@@ -322,7 +363,7 @@ template <int MODE>
 cudaError_t prepare_rowgather(size_t bytes) {
     static size_t configured = 0;
     if (bytes <= configured) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(rowgather_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(rowgather_kernel<MODE, MODE == kModeSpmv ? DPG_GATHER_TILES_SPMV : DPG_GATHER_TILES_PR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(bytes));
     if (e == cudaSuccess) configured = bytes;
     return e;
@@ -400,7 +441,7 @@ cudaError_t launch_spmv(const RowGatherLaunch& L, DevStatus* st, cudaStream_t st
     if (err != cudaSuccess) return err;
     {
         HookScope hs(hook, DPG_KERNEL_ROWGATHER, stream);
-        rowgather_kernel<kModeSpmv><<<gb, bt, smem, stream>>>(L);
+        rowgather_kernel<kModeSpmv, DPG_GATHER_TILES_SPMV><<<gb, bt, smem, stream>>>(L);
     }
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
@@ -421,7 +462,7 @@ cudaError_t launch_pagerank_sweep(const RowGatherLaunch& L, DevStatus* st, cudaS
     if (err != cudaSuccess) return err;
     {
         HookScope hs(hook, DPG_KERNEL_ROWGATHER, stream);
-        rowgather_kernel<kModePagerank><<<gb, bt, smem, stream>>>(L);
+        rowgather_kernel<kModePagerank, DPG_GATHER_TILES_PR><<<gb, bt, smem, stream>>>(L);
     }
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
