@@ -47,7 +47,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["dpg", "reference"], default="dpg")
     ap.add_argument("--no-extra", action="store_true", help="skip the SpMV / SSSP / BFS side measurements")
-    ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs", "adjoint", "prgrad", "batch"],
+    ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs", "adjoint", "prgrad", "batch", "cdp"],
                     default="pagerank",
                     help="pagerank is the headline; the others print their own line (used for profiling)")
     ap.add_argument("--scale", type=int, default=0, help="R-MAT scale for --workload spmv/sssp/bfs")
@@ -495,9 +495,55 @@ def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=51
             "s_generate": t_gen, "s_pack": t_pack, "s_autotune": t_tune, **split}
 
 
+def measure_cdp(dpg, ctx, torch, g, nsrc=3, seed=16):
+    """The reference's recursive BFS variants as CDP2 child launches against the persistent BFS, on
+    the same graph and sources (CUDA events around each synchronous solve)."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    ctx.profile(False)
+    dg = dpg.Graph(ctx, g.offsets, g.col)
+    deg = np.diff(g.offsets)
+    srcs = [int(s) for s in np.random.default_rng(seed).choice(np.flatnonzero(deg > 0), nsrc, replace=False)]
+    lv = torch.empty(g.V, dtype=torch.int32, device=dev)
+    ref = torch.empty(g.V, dtype=torch.int32, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    names = {0: "persistent", dpg.CDP_NAIVE: "cdp_naive", dpg.CDP_WARP: "cdp_warp", dpg.CDP_BLOCK: "cdp_block",
+             dpg.CDP_GRID: "cdp_grid"}
+    for variant, name in names.items():
+        ts, launches, failed, agree = [], 0, 0, True
+        for s in srcs:
+            dpg.bfs_dev(ctx, dg, s, ref.data_ptr())
+            ctx.synchronize()
+            e0.record()
+            try:
+                if variant == 0:
+                    dpg.bfs_dev(ctx, dg, s, lv.data_ptr())
+                    ctx.synchronize()
+                    st = {"launches": 1, "failed_launches": 0}
+                else:
+                    st = dpg.bfs_cdp_dev(ctx, dg, s, variant, lv.data_ptr(), pending_limit=1 << 18)
+            except dpg.DpgError as err:
+                st = {"launches": -1, "failed_launches": -1, "error": str(err)[:120]}
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+            launches += st["launches"]
+            failed += st["failed_launches"]
+            agree = agree and st["failed_launches"] == 0 and bool(torch.equal(lv, ref))
+            if "error" in st:
+                out.setdefault(name + "_error", st["error"])
+        out[name] = {"ms": statistics.median(ts), "launches_per_solve": launches / len(srcs),
+                     "failed_launches": failed, "levels_equal_persistent": agree}
+    base = out["persistent"]["ms"]
+    for name in names.values():
+        out[name]["x_slower_than_persistent"] = out[name]["ms"] / base
+    return out
+
+
 def extra_measurements(dpg, ctx, torch, g, peak, steps):
     """SpMV and the SpMV adjoint on the scale-22 graph; SSSP and BFS on R-MAT scale 24; the PageRank
-    edge-weight gradient on scale 20; the 512-graph batch (device-resident, CUDA events)."""
+    edge-weight gradient on scale 20; the 512-graph batch; the recursive CDP2 BFS variants against
+    the persistent BFS on scale 16 (device-resident, CUDA events)."""
     out = {"spmv_rmat22": measure_spmv(dpg, ctx, torch, g, peak, steps)}
     out["spmv_bwd_rmat22_64rhs"] = measure_adjoint(dpg, ctx, torch, g, peak)
     g24 = dpg.rmat_csr(24, 16, seed=24, wmin=1, wmax=255)
@@ -508,6 +554,7 @@ def extra_measurements(dpg, ctx, torch, g, peak, steps):
     out["pagerank_grad_rmat20"] = measure_prgrad(dpg, ctx, torch, g20, peak)
     del g20
     out["batch_512_graphs"] = measure_batch(dpg, ctx, torch, peak)
+    out["cdp_bfs_rmat16"] = measure_cdp(dpg, ctx, torch, dpg.rmat_csr(16, 16, seed=16, weights=False))
     return out
 
 
@@ -545,6 +592,11 @@ def run_single_workload(args, world=1, rank=0, local=0):
                 return 0
         scale = 0
         g = None
+    elif args.workload == "cdp":
+        scale = args.scale or 16
+        g = dpg.rmat_csr(scale, 16, seed=scale, weights=False)
+        res = measure_cdp(dpg, ctx, torch, g)
+        res["gteps"] = g.E / (res["persistent"]["ms"] / 1e3) / 1e9
     elif args.workload == "prgrad":
         scale = args.scale or 20
         g = dpg.rmat_csr(scale, 16, seed=scale, weights=False)

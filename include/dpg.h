@@ -229,6 +229,22 @@ dpg_status dpg_batch_autotune(dpg_ctx* ctx, dpg_batch* b, int32_t nsrc, const in
  * each part's total cost (nullable). Deterministic: every rank computes the same owners. */
 dpg_status dpg_partition_lpt(int32_t n, const int64_t* cost, int32_t parts, int32_t* owner, int64_t* load);
 
+/* ---- recursive BFS with device-side launches (a measured comparison; replaces nothing) ---------- */
+/* The reference's recursive traversals (bfs_rec_kernel.cu: bfs_kernel_dp 61-89, warp 158-213,
+ * block 305-352, grid 394-457) as CUDA dynamic-parallelism (CDP2) child launches, to be timed
+ * against dpg_bfs. Synchronous. Child launches are limited to 23 generations below the first and
+ * to pending_limit outstanding launches (0: 65536; set as the context's device-runtime limit); a
+ * launch that fails or is skipped makes the call return DPG_ERR_CAPACITY, since its subtree may be
+ * unfinished. Levels are exact when the call succeeds. */
+enum { DPG_CDP_NAIVE = 1, DPG_CDP_WARP = 2, DPG_CDP_BLOCK = 3, DPG_CDP_GRID = 4 };
+typedef struct dpg_cdp_stats {
+    int64_t launches;        /* child grids launched (the reference's nested_calls) */
+    int64_t failed_launches; /* launches that failed or were skipped */
+    int64_t buffer_entries;  /* append-buffer capacity of the consolidated variants */
+} dpg_cdp_stats;
+dpg_status dpg_bfs_cdp_dev(dpg_ctx* ctx, const dpg_graph* g, int32_t source, int32_t variant, int32_t pending_limit,
+                           int32_t* d_level, dpg_cdp_stats* stats);
+
 /* ---- one-shot host calls: the whole reference wrapper in one call (upload, solve, download) ---- */
 dpg_status dpg_sssp_host(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* offsets,
                          const int32_t* col, const int32_t* weights, int32_t source,

@@ -92,6 +92,10 @@ class BatchTuning(ctypes.Structure):
         return {"hub_threshold": self.hub_threshold, "chunk": self.chunk, "pr_hot": self.pr_hot}
 
 
+class CdpStats(ctypes.Structure):
+    _fields_ = [("launches", c_int64), ("failed_launches", c_int64), ("buffer_entries", c_int64)]
+
+
 class RunStats(ctypes.Structure):
     _fields_ = [
         ("iterations", c_int64),
@@ -168,6 +172,7 @@ _SIGS = {
     "dpg_batch_launches": [_P, POINTER(c_int64)],
     "dpg_batch_autotune": [_P, _P, c_int32, _P, _P],
     "dpg_partition_lpt": [c_int32, _P, c_int32, _P, _P],
+    "dpg_bfs_cdp_dev": [_P, _P, c_int32, c_int32, c_int32, _P, _P],
     "dpg_ctx_grad_sweeps": [_P, POINTER(c_int64), POINTER(c_int64)],
     "dpg_write_dimacs9": [c_char_p, c_int32, c_int64, _P, _P, _P, c_int32],
     "dpg_write_cost": [c_char_p, c_int32, c_int32, _P],
@@ -543,6 +548,18 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+CDP_NAIVE, CDP_WARP, CDP_BLOCK, CDP_GRID = 1, 2, 3, 4
+
+
+def bfs_cdp_dev(ctx: Context, g: Graph, source: int, variant: int, d_level: int, pending_limit: int = 0) -> dict:
+    """Recursive BFS with device-side child launches (measured comparison); returns launch counts.
+    Raises DpgError (DPG_ERR_CAPACITY) when a child launch failed or was skipped."""
+    st = CdpStats()
+    _check(lib().dpg_bfs_cdp_dev(ctx.handle, g.handle, source, variant, pending_limit, c_void_p(d_level), byref(st)))
+    return {"launches": int(st.launches), "failed_launches": int(st.failed_launches),
+            "buffer_entries": int(st.buffer_entries)}
 
 
 def partition_lpt(costs, parts: int) -> tuple[np.ndarray, np.ndarray]:

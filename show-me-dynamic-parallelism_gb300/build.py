@@ -30,7 +30,9 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", 
 NVCC_FLAGS += os.environ.get("DPG_NVCC_EXTRA", "").split()
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wextra", "-Wno-unused-parameter"]
 
-LIB_CU = ["dpg_api.cu", "dpg_expand.cu", "dpg_rowgather.cu", "dpg_noalloc.cu", "dpg_layout.cu", "dpg_adjoint.cu", "dpg_prgrad.cu", "dpg_batch.cu"]
+LIB_CU = ["dpg_api.cu", "dpg_expand.cu", "dpg_rowgather.cu", "dpg_noalloc.cu", "dpg_layout.cu", "dpg_adjoint.cu", "dpg_prgrad.cu", "dpg_batch.cu", "dpg_cdp.cu"]
+# Translation units with device-side launches (relocatable device code, linked with cudadevrt).
+RDC_CU = {"dpg_cdp.cu"}
 LIB_CXX = ["dpg_host.cpp"]
 # app name -> source file (apps link against libdpg.so)
 APP_SOURCES = {
@@ -84,7 +86,8 @@ def build(force: bool = False, verbose: bool = False, apps: bool = True) -> Path
         obj = BUILD / (name + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
-            jobs.append([nvcc(), *ARCH, *NVCC_FLAGS, f"-I{INCLUDE}", f"-I{CSRC}", "-c", str(src), "-o", str(obj)])
+            rdc = ["-rdc=true"] if name in RDC_CU else []
+            jobs.append([nvcc(), *ARCH, *NVCC_FLAGS, *rdc, f"-I{INCLUDE}", f"-I{CSRC}", "-c", str(src), "-o", str(obj)])
     for name in LIB_CXX:
         src = CSRC / name
         obj = BUILD / (name + ".o")
@@ -96,7 +99,9 @@ def build(force: bool = False, verbose: bool = False, apps: bool = True) -> Path
         list(ex.map(lambda c: _run(c, verbose), jobs))
     if force or jobs or _stale(LIB, objs):
         tmp = LIB.with_suffix(".so.tmp")
-        _run([nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fopenmp", "-lgomp"], verbose)
+        # -rdc=true links the relocatable device code of RDC_CU against the device runtime.
+        _run([nvcc(), *ARCH, "-shared", "-rdc=true", "-o", str(tmp), *map(str, objs), "-lcudadevrt", "-Xcompiler",
+              "-fopenmp", "-lgomp"], verbose)
         os.replace(tmp, LIB)
     if apps and APPS.exists():
         BIN.mkdir(exist_ok=True)

@@ -124,6 +124,7 @@ dpg_status graph_finish(dpg_ctx* c, dpg_graph* g, const int32_t* d_w_src) {
 
 void graph_free_device(dpg_graph* g) {
     if (g->tgraph) {
+        if (g->tgraph->ctx) g->tgraph->ctx->graphs.erase(g->tgraph);
         graph_free_device(g->tgraph);
         delete g->tgraph;
         g->tgraph = nullptr;
@@ -595,6 +596,7 @@ dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* 
     if (!offsets || (E > 0 && !col)) return set_error(DPG_ERR_INVALID_ARG, "null offsets or columns");
     dpg_graph* g = new dpg_graph();
     g->ctx = c;
+    g->device = c->device;
     g->V = V;
     g->E = E;
     g->weighted = weights != nullptr;
@@ -637,6 +639,7 @@ dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* 
     }
     s = graph_finish(c, g, d_w);
     if (s != DPG_OK) return fail(s);
+    c->graphs.insert(g);
     *out = g;
     return DPG_OK;
 }
@@ -809,6 +812,8 @@ dpg_status dpg_ctx_destroy(dpg_ctx* c) {
     if (!c) return DPG_OK;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    for (dpg_graph* g : c->graphs) g->ctx = nullptr;
+    for (dpg_batch* b : c->batches) batch_orphan(b);
     for (auto& b : c->bufs) cudaFree(b.p);
     cudaFree(c->st);
     cudaFree(c->trace);
@@ -907,8 +912,13 @@ dpg_status dpg_graph_create_device(dpg_ctx* c, int32_t V, int64_t E, const int32
 
 dpg_status dpg_graph_destroy(dpg_graph* g) {
     if (!g) return DPG_OK;
-    cudaSetDevice(g->ctx->device);
-    cudaStreamSynchronize(g->ctx->stream);
+    if (g->ctx) {
+        cudaSetDevice(g->ctx->device);
+        cudaStreamSynchronize(g->ctx->stream);
+        g->ctx->graphs.erase(g);
+    } else {
+        cudaSetDevice(g->device);  // orphaned by dpg_ctx_destroy: only the memory is left to free
+    }
     graph_free_device(g);
     delete g;
     return DPG_OK;
@@ -1032,6 +1042,48 @@ dpg_status dpg_ctx_grad_sweeps(const dpg_ctx* c, int64_t* forward, int64_t* adjo
     if (!c) return set_error(DPG_ERR_INVALID_ARG, "null context");
     if (forward) *forward = c->last_grad_sweeps[0];
     if (adjoint) *adjoint = c->last_grad_sweeps[1];
+    return DPG_OK;
+}
+
+dpg_status dpg_bfs_cdp_dev(dpg_ctx* c, const dpg_graph* g, int32_t source, int32_t variant, int32_t pending_limit,
+                           int32_t* d_level, dpg_cdp_stats* stats) {
+    DPG_TRY(use_device(c));
+    if (!g || g->ctx != c) return set_error(DPG_ERR_INVALID_ARG, "graph does not belong to this context");
+    if (source < 0 || source >= g->V || !d_level) return set_error(DPG_ERR_INVALID_ARG, "bad source or null output");
+    if (variant < DPG_CDP_NAIVE || variant > DPG_CDP_GRID) return set_error(DPG_ERR_INVALID_ARG, "unknown variant");
+    if (pending_limit < 0) return set_error(DPG_ERR_INVALID_ARG, "pending_limit must be >= 0");
+    const size_t want = static_cast<size_t>(pending_limit > 0 ? pending_limit : 65536);
+    size_t have = 0;
+    DPG_CUDA_TRY(cudaDeviceGetLimit(&have, cudaLimitDevRuntimePendingLaunchCount));
+    if (have != want) {
+        DPG_CUDA_TRY(cudaDeviceSynchronize());
+        DPG_CUDA_TRY(cudaDeviceSetLimit(cudaLimitDevRuntimePendingLaunchCount, want));
+    }
+    const size_t cap = cdp_buffer_entries(g->E, g->V);
+    dpg_status st = DPG_OK;
+    unsigned* b0 = static_cast<unsigned*>(arena(c, S_CDP_BUF0, cap * 4, &st));
+    unsigned* b1 = static_cast<unsigned*>(arena(c, S_CDP_BUF1, cap * 4, &st));
+    unsigned* words = static_cast<unsigned*>(arena(c, S_CDP_WORDS, 4 * 4 + sizeof(CdpCounters), &st));
+    if (st != DPG_OK) return st;
+    CdpCounters* ct = reinterpret_cast<CdpCounters*>(words + 4);
+    c->last_host_iterations = -1;
+    {
+        HookScope hs(&c->prof, DPG_KERNEL_EXPAND, c->stream);
+        DPG_CUDA_TRY(launch_bfs_cdp(variant, g->off, g->col, g->V, source, d_level, b0, b1, cap, words, ct, c->stream,
+                                    c->sm_count));
+    }
+    CdpCounters h{};
+    DPG_CUDA_TRY(cudaMemcpyAsync(&h, ct, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (stats) {
+        stats->launches = static_cast<int64_t>(h.launches);
+        stats->failed_launches = static_cast<int64_t>(h.failures);
+        stats->buffer_entries = static_cast<int64_t>(cap);
+    }
+    if (h.failures)
+        return set_error(DPG_ERR_CAPACITY, std::to_string(h.failures) +
+                                               " child launches failed or were skipped (nesting depth, pending-launch "
+                                               "limit or buffer); levels are incomplete");
     return DPG_OK;
 }
 

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <unordered_set>
 #include <vector>
 
 #include "dpg_internal.h"
@@ -32,6 +33,7 @@ enum Slot {
     S_PARTIAL, S_DPART, S_DFIX, S_DSUM, S_NONSTOP, S_VALS, S_X, S_Y, S_OUTDEG, S_RANKOUT, S_XPERM, S_PENDING, S_SPMM_PARTIAL, S_VALS_T,
     S_PRG_W, S_PRG_Y, S_PRG_C, S_PRG_V0, S_PRG_V1, S_PRG_V2, S_PRG_V3, S_PRG_PART, S_PRG_RED, S_PRG_FLAGS,
     S_DIRTY0, S_DIRTY1,
+    S_CDP_BUF0, S_CDP_BUF1, S_CDP_WORDS,
     S_COUNT_SLOTS
 };
 
@@ -123,10 +125,15 @@ struct dpg_ctx {
     Profiler prof;
     unsigned long long* trace = nullptr;  // per-iteration expansion trace (dpg_ctx_trace_enable)
     int32_t trace_cap = 0;
+    // Graphs and batches created on this context. Destroying the context orphans them (their ctx
+    // becomes null) so that destroying them afterwards frees their memory without touching it.
+    std::unordered_set<dpg_graph*> graphs;
+    std::unordered_set<dpg_batch*> batches;
 };
 
 struct dpg_graph {
-    dpg_ctx* ctx = nullptr;
+    dpg_ctx* ctx = nullptr;  // null once the context was destroyed
+    int device = 0;
     int32_t V = 0;
     int64_t E = 0;
     bool weighted = false;
@@ -171,6 +178,7 @@ dpg_status ensure_plan(dpg_graph* g);
 dpg_status ensure_relabel(dpg_graph* g);
 int32_t hot_entries(const dpg_ctx* c, const dpg_graph* g);
 dpg_status pr_defaults(const dpg_pr_opts* in, dpg_pr_opts* o);
+void batch_orphan(dpg_batch* b);
 dpg_status expand_workspace(dpg_ctx* c, int32_t V, int64_t E, int32_t min_chunked, ExpandWorkspace* wsp);
 void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const dpg_graph* g);
 

@@ -91,7 +91,8 @@ __global__ void __launch_bounds__(kBlk) batch_dangling_kernel(const int4* __rest
 }  // namespace
 
 struct dpg_batch {
-    dpg_ctx* ctx = nullptr;
+    dpg_ctx* ctx = nullptr;  // null once the context was destroyed
+    int device = 0;
     int32_t n = 0;
     int32_t V = 0;
     int64_t E = 0;
@@ -382,6 +383,10 @@ float time_ms(dpg_ctx* c, const std::function<dpg_status()>& fn, int reps, dpg_s
 
 }  // namespace
 
+namespace dpg_api {
+void batch_orphan(dpg_batch* b) { b->ctx = nullptr; }
+}  // namespace dpg_api
+
 extern "C" {
 
 dpg_status dpg_batch_create(dpg_ctx* c, int32_t ngraphs, const int32_t* vstart, int64_t E, const int32_t* offsets,
@@ -417,6 +422,7 @@ dpg_status dpg_batch_create(dpg_ctx* c, int32_t ngraphs, const int32_t* vstart, 
                                                   " has an arc leaving its vertex range (or decreasing offsets)");
     dpg_batch* b = new dpg_batch();
     b->ctx = c;
+    b->device = c->device;
     b->n = ngraphs;
     b->V = V;
     b->E = E;
@@ -478,14 +484,20 @@ dpg_status dpg_batch_create(dpg_ctx* c, int32_t ngraphs, const int32_t* vstart, 
     if (e == cudaSuccess) e = cudaMemsetAsync(b->ticket, 0, sizeof(unsigned) * 4, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return fail(set_error(DPG_ERR_CUDA, std::string("batch buffers: ") + cudaGetErrorString(e)));
+    c->batches.insert(b);
     *out = b;
     return DPG_OK;
 }
 
 dpg_status dpg_batch_destroy(dpg_batch* b) {
     if (!b) return DPG_OK;
-    cudaSetDevice(b->ctx->device);
-    cudaStreamSynchronize(b->ctx->stream);
+    if (b->ctx) {
+        cudaSetDevice(b->ctx->device);
+        cudaStreamSynchronize(b->ctx->stream);
+        b->ctx->batches.erase(b);
+    } else {
+        cudaSetDevice(b->device);  // orphaned by dpg_ctx_destroy: only the memory is left to free
+    }
     batch_free(b);
     delete b;
     return DPG_OK;

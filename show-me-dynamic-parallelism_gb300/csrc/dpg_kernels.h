@@ -193,6 +193,18 @@ cudaError_t launch_arc_dot(const SpmmPlanDev& P, const int32_t* col, const float
 cudaError_t launch_gather_values(const float* v, const int32_t* idx, int64_t n, float* out, cudaStream_t s,
                                  int sm_count);
 
+// ---- recursive BFS with device-side launches (dpg_cdp.cu, relocatable device code) --------------
+struct CdpCounters {
+    unsigned long long launches;  // child grids launched
+    unsigned long long failures;  // launches that failed or were skipped (depth, buffer)
+};
+// Append-buffer entries the consolidated variants get for a graph of V vertices and E arcs.
+size_t cdp_buffer_entries(int64_t E, int32_t V);
+// Runs variant DPG_CDP_* from source; buffer and buffer2 hold cap entries each, words 4 unsigned.
+cudaError_t launch_bfs_cdp(int variant, const int32_t* off, const int32_t* col, int32_t V, int32_t source,
+                           int32_t* level, unsigned* buffer, unsigned* buffer2, size_t cap, unsigned* words,
+                           CdpCounters* ct, cudaStream_t s, int sm_count);
+
 // ---- weighted PageRank and its edge-weight gradient (dpg_prgrad.cu) ------------------------------
 
 enum PrVecMode {
