@@ -314,6 +314,14 @@ typedef struct dpg_host_graph {
  * vertex's neighbour order reversed with respect to the file, DIMACS10/SLNDC weights drawn with
  * srand(7); rand()%1000+1. */
 dpg_status dpg_read_graph(const char* path, int32_t format, dpg_host_graph* out);
+/* The same with an explicit thread count: DIMACS9 files are parsed in parallel over line-aligned
+ * chunks (threads = 0: all OpenMP threads; 1: the serial reader). Results, including the first
+ * error reported, are identical either way. */
+dpg_status dpg_read_graph_ex(const char* path, int32_t format, int32_t threads, dpg_host_graph* out);
+/* Binary CSR cache of a loaded graph ("DPGCSR01", V, E, source, offsets, col, weights): a reload
+ * skips parsing and CSR construction. */
+dpg_status dpg_write_graph_cache(const char* path, const dpg_host_graph* g);
+dpg_status dpg_read_graph_cache(const char* path, dpg_host_graph* out);
 void dpg_host_graph_free(dpg_host_graph* g);
 /* convertCSR on an in-memory arc list in file order (global.cpp:192-235). Outputs are caller-owned. */
 dpg_status dpg_csr_from_arcs(int32_t V, int64_t E, const int32_t* src, const int32_t* dst,
@@ -321,6 +329,12 @@ dpg_status dpg_csr_from_arcs(int32_t V, int64_t E, const int32_t* src, const int
 /* invertGraph (global.cpp:237-277): transposed CSR in the reference's neighbour order. */
 dpg_status dpg_csr_transpose(int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
                              int32_t* in_offsets, int32_t* in_col);
+/* The same on the device (replaces invertGraph, global.cpp:237-277): identical arrays, built with a
+ * stable radix sort of the arcs by head; d_in_arc (nullable) receives the arc permutation. The input
+ * is checked on the device first (offsets rising from 0 to E, columns in [0, V)), so the call
+ * synchronises once; the transpose itself is stream-ordered on the context's stream. */
+dpg_status dpg_csr_transpose_dev(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* d_offsets, const int32_t* d_col,
+                                 int32_t* d_in_offsets, int32_t* d_in_col, int32_t* d_in_arc);
 /* Same, and in_arc[p] = index in col of the arc that transposed slot p came from. */
 dpg_status dpg_csr_transpose_perm(int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
                                   int32_t* in_offsets, int32_t* in_col, int32_t* in_arc);

@@ -154,6 +154,9 @@ _SIGS = {
     "dpg_selftest_barrier_timeout": [_P, c_double],
     "dpg_sssp_noalloc_dev": [c_int32, c_int64, _P, _P, c_int32, _P, _P],
     "dpg_read_graph": [c_char_p, c_int32, POINTER(_HostGraph)],
+    "dpg_read_graph_ex": [c_char_p, c_int32, c_int32, POINTER(_HostGraph)],
+    "dpg_write_graph_cache": [c_char_p, POINTER(_HostGraph)],
+    "dpg_read_graph_cache": [c_char_p, POINTER(_HostGraph)],
     "dpg_host_graph_free": [POINTER(_HostGraph)],
     "dpg_csr_from_arcs": [c_int32, c_int64, _P, _P, _P, _P, _P, _P],
     "dpg_csr_transpose": [c_int32, c_int64, _P, _P, _P, _P],
@@ -173,6 +176,7 @@ _SIGS = {
     "dpg_batch_autotune": [_P, _P, c_int32, _P, _P],
     "dpg_partition_lpt": [c_int32, _P, c_int32, _P, _P],
     "dpg_bfs_cdp_dev": [_P, _P, c_int32, c_int32, c_int32, _P, _P],
+    "dpg_csr_transpose_dev": [_P, c_int32, c_int64, _P, _P, _P, _P, _P],
     "dpg_ctx_grad_sweeps": [_P, POINTER(c_int64), POINTER(c_int64)],
     "dpg_write_dimacs9": [c_char_p, c_int32, c_int64, _P, _P, _P, c_int32],
     "dpg_write_cost": [c_char_p, c_int32, c_int32, _P],
@@ -240,10 +244,7 @@ class CSR(NamedTuple):
     weights: np.ndarray | None
 
 
-def read_graph(path: str | Path, fmt: int = 0) -> CSR:
-    """readInputDIMACS9/10/SLNDC + convertCSR (common/global.cpp:29-235); fmt is the apps' -f flag."""
-    hg = _HostGraph()
-    _check(lib().dpg_read_graph(str(path).encode(), fmt, byref(hg)))
+def _host_to_csr(hg) -> CSR:
     try:
         V, E = hg.V, hg.E
         off = np.ctypeslib.as_array(hg.offsets, shape=(V + 1,)).copy()
@@ -252,6 +253,32 @@ def read_graph(path: str | Path, fmt: int = 0) -> CSR:
         return CSR(V, E, hg.source, off, col, w)
     finally:
         lib().dpg_host_graph_free(byref(hg))
+
+
+def read_graph(path: str | Path, fmt: int = 0, threads: int = 0) -> CSR:
+    """readInputDIMACS9/10/SLNDC + convertCSR (common/global.cpp:29-235); fmt is the apps' -f flag.
+    DIMACS9 is parsed in parallel unless threads == 1 (identical results)."""
+    hg = _HostGraph()
+    _check(lib().dpg_read_graph_ex(str(path).encode(), fmt, threads, byref(hg)))
+    return _host_to_csr(hg)
+
+
+def write_graph_cache(path: str | Path, g: CSR) -> None:
+    """Binary CSR cache of g (offsets, columns, weights, source)."""
+    off, col = _i32(g.offsets), _i32(g.col)
+    w = _i32(g.weights) if g.weights is not None else None
+    hg = _HostGraph()
+    hg.V, hg.E, hg.source = g.V, g.E, g.source
+    hg.offsets = off.ctypes.data_as(POINTER(c_int32))
+    hg.col = col.ctypes.data_as(POINTER(c_int32))
+    hg.weights = w.ctypes.data_as(POINTER(c_int32)) if w is not None else None
+    _check(lib().dpg_write_graph_cache(str(path).encode(), byref(hg)))
+
+
+def read_graph_cache(path: str | Path) -> CSR:
+    hg = _HostGraph()
+    _check(lib().dpg_read_graph_cache(str(path).encode(), byref(hg)))
+    return _host_to_csr(hg)
 
 
 def csr_from_arcs(V: int, src, dst, w=None) -> CSR:
@@ -665,6 +692,13 @@ def pagerank_grad_dev(ctx: Context, g: Graph, d_weights: int, d_seed: int, d_ran
     f, a = c_int64(0), c_int64(0)
     _check(lib().dpg_ctx_grad_sweeps(ctx.handle, byref(f), byref(a)))
     return int(f.value), int(a.value)
+
+
+def csr_transpose_dev(ctx: Context, V: int, E: int, d_offsets: int, d_col: int, d_in_offsets: int, d_in_col: int,
+                      d_in_arc: int | None = None) -> None:
+    """invertGraph on the device (device pointers; stream-ordered)."""
+    _check(lib().dpg_csr_transpose_dev(ctx.handle, V, E, c_void_p(d_offsets), c_void_p(d_col), c_void_p(d_in_offsets),
+                                       c_void_p(d_in_col), c_void_p(d_in_arc) if d_in_arc else None))
 
 
 def csr_transpose_perm(V: int, offsets, col):

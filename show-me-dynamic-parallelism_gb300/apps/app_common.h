@@ -10,6 +10,10 @@
 // apps/bfs-rec/src/bfs_rec.cpp:130-141 does).
 #pragma once
 
+#include <sys/stat.h>
+
+#include <string>
+
 #include <sys/time.h>
 
 #include <cstdio>
@@ -28,6 +32,7 @@ struct AppConf {
     int source_1based = 0;  // 0: from the file
     const char* out_file = nullptr;
     bool verify = false;
+    bool cache = false;  // --cache: reuse <graph file>.dpgcsr when newer than the file
     double damping = -1.0;  // PageRank overrides (< 0: reference default)
     int iterations = -1;
 };
@@ -75,6 +80,8 @@ inline int app_parse(int argc, char** argv, AppConf* c, void (*usage)()) {
             c->out_file = next();
         } else if (!strcmp(a, "--verify")) {
             c->verify = true;
+        } else if (!strcmp(a, "--cache")) {
+            c->cache = true;
         } else if (!strcmp(a, "--damping")) {
             const char* v = next();
             c->damping = v ? atof(v) : -1.0;
@@ -118,6 +125,7 @@ inline void app_usage_tail() {
     fprintf(stderr, "    --source <number>                  source vertex (1-based; default: the file's s line)\n");
     fprintf(stderr, "    --out <file>                       write the result in the reference's text format\n");
     fprintf(stderr, "    --verify                           check against a CPU restatement (PASS/ERROR)\n");
+    fprintf(stderr, "    --cache                            keep a binary CSR next to the input and reuse it\n");
 }
 
 // Loads the graph with the reference reader semantics and prints the reference's progress lines.
@@ -130,7 +138,19 @@ inline int app_load(const AppConf& c, dpg_host_graph* g, bool print_source, doub
     }
     fclose(probe);
     const double t0 = app_gettime();
-    dpg_status s = dpg_read_graph(c.graph_file, c.data_set_format, g);
+    dpg_status s = DPG_ERR_IO;
+    std::string cache_path = std::string(c.graph_file) + ".dpgcsr";
+    bool from_cache = false;
+    if (c.cache) {
+        struct stat sf, sc;
+        if (stat(c.graph_file, &sf) == 0 && stat(cache_path.c_str(), &sc) == 0 && sc.st_mtime >= sf.st_mtime) {
+            s = dpg_read_graph_cache(cache_path.c_str(), g);
+            from_cache = s == DPG_OK;
+        }
+    }
+    if (!from_cache) s = dpg_read_graph(c.graph_file, c.data_set_format, g);
+    if (c.cache && !from_cache && s == DPG_OK && dpg_write_graph_cache(cache_path.c_str(), g) != DPG_OK)
+        fprintf(stderr, "Warning: %s\n", dpg_last_error());
     const double t1 = app_gettime();
     if (s != DPG_OK) {
         fprintf(stderr, "Error: %s\n", dpg_last_error());

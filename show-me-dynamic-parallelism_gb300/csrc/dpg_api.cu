@@ -86,6 +86,15 @@ __global__ void validate_interleave_kernel(const int32_t* col, const int32_t* w,
     }
 }
 
+// Device-side check of a CSR given by device pointers: bad |= 4 when the offsets do not rise from 0
+// to E (the columns are checked by validate_interleave_kernel).
+__global__ void validate_offsets_kernel(const int32_t* off, int32_t V, int64_t E, int* bad) {
+    for (int64_t v = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; v < V;
+         v += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        if (off[v + 1] < off[v]) atomicOr(bad, 4);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (off[0] != 0 || static_cast<int64_t>(off[V]) != E)) atomicOr(bad, 4);
+}
+
 dpg_status validate_offsets(const int32_t* off, int32_t V, int64_t E, int32_t* max_deg) {
     if (off[0] != 0 || static_cast<int64_t>(off[V]) != E)
         return set_error(DPG_ERR_INVALID_ARG, "offsets must start at 0 and end at E");
@@ -279,31 +288,44 @@ dpg_status ensure_spmm_plan(dpg_graph* g) {
     return DPG_OK;
 }
 
-// Deterministic transposed CSR with the arc permutation: the columns come back to the host once,
-// dpg_csr_transpose_perm orders them as invertGraph does, and the result goes back up. With
+// Deterministic transposed CSR with the arc permutation, built on the device in invertGraph order
+// (dpg_transpose.cu); only its offsets come back to the host, for the batched-RHS plan. With
 // need_graph the transposed CSR also becomes a graph of its own (g->tgraph).
 dpg_status ensure_spmm_transpose(dpg_graph* g, bool need_graph = false) {
     if (g->spmm_t_ready && (!need_graph || g->tgraph)) return DPG_OK;
     dpg_ctx* c = g->ctx;
     const size_t nv = static_cast<size_t>(g->V), ne = static_cast<size_t>(g->E > 0 ? g->E : 1);
-    std::vector<int32_t> h_col(ne), t_off(nv + 1), t_col(ne), t_arc(ne);
-    if (g->E > 0) DPG_CUDA_TRY(cudaMemcpy(h_col.data(), g->col, static_cast<size_t>(g->E) * 4, cudaMemcpyDeviceToHost));
-    DPG_TRY(dpg_csr_transpose_perm(g->V, g->E, g->h_off.data(), h_col.data(), t_off.data(), t_col.data(), t_arc.data()));
+    int32_t* t_off = nullptr;
+    DPG_CUDA_TRY(cudaMalloc(&t_off, (nv + 1) * 4));
+    cudaError_t e = cudaSuccess;
+    if (!g->tt_col) e = cudaMalloc(&g->tt_col, ne * 4);
+    if (e == cudaSuccess && !g->tt_arc) e = cudaMalloc(&g->tt_arc, ne * 4);
+    dpg_status st = DPG_OK;
+    const size_t scratch_bytes = transpose_scratch_bytes(g->V, g->E);
+    void* scratch = e == cudaSuccess ? arena(c, S_TRANSPOSE, scratch_bytes, &st) : nullptr;
+    if (e == cudaSuccess && st == DPG_OK)
+        e = launch_transpose(g->off, g->col, g->V, g->E, t_off, g->tt_col, g->tt_arc, scratch, scratch_bytes,
+                             c->stream, c->sm_count);
+    std::vector<int32_t> h_t_off(nv + 1);
+    if (e == cudaSuccess && st == DPG_OK)
+        e = cudaMemcpyAsync(h_t_off.data(), t_off, (nv + 1) * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && st == DPG_OK) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess || st != DPG_OK) {
+        cudaFree(t_off);
+        return st != DPG_OK ? st : set_error(DPG_ERR_CUDA, std::string("device transpose: ") + cudaGetErrorString(e));
+    }
     if (!g->spmm_t_ready) {
-        DPG_CUDA_TRY(cudaMalloc(&g->tt_col, ne * 4));
-        DPG_CUDA_TRY(cudaMalloc(&g->tt_arc, ne * 4));
-        DPG_CUDA_TRY(cudaMemcpyAsync(g->tt_col, t_col.data(), ne * 4, cudaMemcpyHostToDevice, c->stream));
-        DPG_CUDA_TRY(cudaMemcpyAsync(g->tt_arc, t_arc.data(), ne * 4, cudaMemcpyHostToDevice, c->stream));
         SpmmPlanHost hp;
-        build_spmm_plan(t_off.data(), g->V, &hp);
-        DPG_TRY(upload_spmm_plan(c, hp, &g->spmm_t_plan));
-        g->spmm_t_ready = true;
+        build_spmm_plan(h_t_off.data(), g->V, &hp);
+        st = upload_spmm_plan(c, hp, &g->spmm_t_plan);
+        if (st == DPG_OK) g->spmm_t_ready = true;
     }
-    if (need_graph && !g->tgraph) {
-        DPG_TRY(graph_create_common(c, g->V, g->E, t_off.data(), t_col.data(), nullptr, false, &g->tgraph));
-        g->tgraph->relabel = g->relabel;
+    if (st == DPG_OK && need_graph && !g->tgraph) {
+        st = graph_create_common(c, g->V, g->E, t_off, g->tt_col, nullptr, true, &g->tgraph);
+        if (st == DPG_OK) g->tgraph->relabel = g->relabel;
     }
-    return DPG_OK;
+    cudaFree(t_off);
+    return st;
 }
 
 dpg_status check_nrhs(int32_t nrhs) {
@@ -1084,6 +1106,34 @@ dpg_status dpg_bfs_cdp_dev(dpg_ctx* c, const dpg_graph* g, int32_t source, int32
         return set_error(DPG_ERR_CAPACITY, std::to_string(h.failures) +
                                                " child launches failed or were skipped (nesting depth, pending-launch "
                                                "limit or buffer); levels are incomplete");
+    return DPG_OK;
+}
+
+dpg_status dpg_csr_transpose_dev(dpg_ctx* c, int32_t V, int64_t E, const int32_t* d_offsets, const int32_t* d_col,
+                                 int32_t* d_in_offsets, int32_t* d_in_col, int32_t* d_in_arc) {
+    DPG_TRY(use_device(c));
+    if (V < 0 || E < 0 || E > INT32_MAX) return set_error(DPG_ERR_INVALID_ARG, "V must be >= 0 and 0 <= E < 2^31");
+    if (!d_offsets || !d_in_offsets || (E > 0 && (!d_col || !d_in_col)))
+        return set_error(DPG_ERR_INVALID_ARG, "null offsets or columns");
+    dpg_status st = DPG_OK;
+    int* bad = static_cast<int*>(arena(c, S_NONSTOP, sizeof(int) * 4, &st));
+    if (st != DPG_OK) return st;
+    DPG_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), c->stream));
+    validate_offsets_kernel<<<c->sm_count * 4, 256, 0, c->stream>>>(d_offsets, V, E, bad);
+    if (E > 0) validate_interleave_kernel<<<c->sm_count * 4, 256, 0, c->stream>>>(d_col, nullptr, nullptr, E, V, bad);
+    DPG_CUDA_TRY(cudaGetLastError());
+    int hbad = 0;
+    DPG_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (hbad & 4) return set_error(DPG_ERR_INVALID_ARG, "offsets must rise from 0 to E");
+    if (hbad & 1) return set_error(DPG_ERR_INVALID_ARG, "column index out of range");
+    const size_t scratch_bytes = transpose_scratch_bytes(V, E);
+    void* scratch = arena(c, S_TRANSPOSE, scratch_bytes, &st);
+    int32_t* arc = d_in_arc ? d_in_arc
+                            : static_cast<int32_t*>(arena(c, S_TRANSPOSE_ARC, static_cast<size_t>(E > 0 ? E : 1) * 4, &st));
+    if (st != DPG_OK) return st;
+    DPG_CUDA_TRY(launch_transpose(d_offsets, d_col, V, E, d_in_offsets, d_in_col, arc, scratch, scratch_bytes, c->stream,
+                                  c->sm_count));
     return DPG_OK;
 }
 

@@ -13,6 +13,10 @@
 
 #include "dpg_internal.h"
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 #include <algorithm>
 #include <cerrno>
 #include <cinttypes>
@@ -21,6 +25,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace dpg {
@@ -148,6 +153,187 @@ dpg_status read_dimacs9(FILE* fp, ArcList* g) {
     if (g->V > 0 && (g->source < 0 || g->source >= g->V))
         return set_error(DPG_ERR_FORMAT, "source vertex out of range");
     return DPG_OK;
+}
+
+// The same DIMACS9 reader over the whole file held in memory, in parallel. The file is cut into
+// chunks at line boundaries; every thread runs the serial reader's per-line code (the same token
+// splitting and atoi-like parsing) over its lines; the arcs are joined in file order. Shapes whose
+// semantics depend on line order beyond that (several 'p' lines, a line longer than the serial
+// reader's buffer) return false so that the caller runs the serial reader instead.
+struct ChunkArcs {
+    std::vector<int32_t> src, dst, w;  // 1-based endpoints as read, range-checked after the join
+    std::vector<int64_t> arc_pos;      // byte position of each arc line (for the first range error)
+    int64_t err_pos = INT64_MAX;
+    std::string err;
+    std::vector<std::pair<int64_t, std::pair<long long, long long>>> p_lines;  // (pos, (V, E))
+    int64_t s_pos = -1;
+    long long s_val = 0;
+    int64_t first_a = INT64_MAX;
+};
+
+bool read_dimacs9_parallel(char* buf, int64_t n, int threads, ArcList* g, dpg_status* status) {
+    // Longest line check (the serial reader's fgets splits lines of kLineBuf - 1 characters or more).
+    std::vector<int64_t> cut(static_cast<size_t>(threads) + 1, n);
+    cut[0] = 0;
+    for (int t = 1; t < threads; ++t) {
+        int64_t c = n * t / threads;
+        while (c < n && buf[c - 1] != '\n') ++c;
+        cut[t] = std::max(c, cut[t - 1]);
+    }
+    std::vector<ChunkArcs> part(static_cast<size_t>(threads));
+    bool too_long = false;
+#pragma omp parallel for num_threads(threads) schedule(static, 1) reduction(|| : too_long)
+    for (int t = 0; t < threads; ++t) {
+        ChunkArcs& R = part[t];
+        std::vector<char*> toks;
+        const size_t guess = static_cast<size_t>((cut[t + 1] - cut[t]) / 12 + 16);
+        R.src.reserve(guess);
+        R.dst.reserve(guess);
+        R.w.reserve(guess);
+        R.arc_pos.reserve(guess);
+        int64_t pos = cut[t];
+        while (pos < cut[t + 1]) {
+            int64_t end = pos;
+            while (end < cut[t + 1] && buf[end] != '\n') ++end;
+            if (end - pos + 1 >= static_cast<int64_t>(kLineBuf) - 1) too_long = true;
+            const int64_t next = end + 1;
+            char saved = end < n ? buf[end] : 0;
+            if (end < n) buf[end] = 0;
+            char* line = buf + pos;
+            if (R.err_pos == INT64_MAX && !too_long) {
+                if (line[0] == 'p') {
+                    long long V = 0, E = 0;
+                    if (strlen(line) < 4) {
+                        R.err_pos = pos;
+                        R.err = "short 'p' line";
+                    } else {
+                        split_spaces(line + 4, &toks);
+                        if (toks.size() < 2 || !parse_int_token(toks[0], &V) || !parse_int_token(toks[1], &E) ||
+                            V < 0 || E < 0 || V > INT32_MAX || E > INT64_MAX / 2) {
+                            R.err_pos = pos;
+                            R.err = "bad 'p' line";
+                        } else {
+                            R.p_lines.push_back({pos, {V, E}});
+                        }
+                    }
+                } else if (line[0] == 's') {
+                    split_spaces(line + 1, &toks);
+                    long long sv = 0;
+                    if (toks.empty() || !parse_int_token(toks[0], &sv)) {
+                        R.err_pos = pos;
+                        R.err = "bad 's' line";
+                    } else {
+                        R.s_pos = pos;
+                        R.s_val = sv;
+                    }
+                } else if (line[0] == 'a') {
+                    if (R.first_a == INT64_MAX) R.first_a = pos;
+                    split_spaces(line + 1, &toks);
+                    long long a = 0, h = 0, wt = 0;
+                    if (toks.size() < 3 || !parse_int_token(toks[0], &a) || !parse_int_token(toks[1], &h) ||
+                        !parse_int_token(toks[2], &wt)) {
+                        R.err_pos = pos;
+                        R.err = "bad 'a' line";
+                    } else if (a < 1 || a > INT32_MAX || h < 1 || h > INT32_MAX) {
+                        R.err_pos = pos;
+                        R.err = "arc endpoint out of range";
+                    } else if (wt < INT32_MIN || wt > INT32_MAX) {
+                        R.err_pos = pos;
+                        R.err = "weight out of int32 range";
+                    } else {
+                        R.src.push_back(static_cast<int32_t>(a));
+                        R.dst.push_back(static_cast<int32_t>(h));
+                        R.w.push_back(static_cast<int32_t>(wt));
+                        R.arc_pos.push_back(pos);
+                    }
+                }
+            }
+            if (end < n) buf[end] = saved;
+            pos = next;
+        }
+    }
+    if (too_long) return false;
+    int np = 0;
+    int64_t p_pos = INT64_MAX, first_a = INT64_MAX, err_pos = INT64_MAX, s_pos = -1;
+    long long V = 0, declared = 0, s_val = 1;
+    std::string err;
+    for (const ChunkArcs& R : part) {
+        np += static_cast<int>(R.p_lines.size());
+        for (auto& pl : R.p_lines) {
+            p_pos = pl.first;
+            V = pl.second.first;
+            declared = pl.second.second;
+        }
+        first_a = std::min(first_a, R.first_a);
+        if (R.err_pos < err_pos) {
+            err_pos = R.err_pos;
+            err = R.err;
+        }
+        if (R.s_pos > s_pos) {
+            s_pos = R.s_pos;
+            s_val = R.s_val;
+        }
+    }
+    if (np > 1) return false;
+    // The serial reader stops at the first failing line in file order.
+    if (np == 1 && first_a < p_pos && first_a < err_pos) {
+        err_pos = first_a;
+        err = "'a' line before 'p' line";
+    }
+    if (np == 0 && first_a < err_pos) {
+        err_pos = first_a;
+        err = "'a' line before 'p' line";
+    }
+    // Endpoint range against V: the first out-of-range arc line in file order.
+    for (const ChunkArcs& R : part) {
+        bool found = false;
+        for (size_t k = 0; k < R.src.size() && R.arc_pos[k] < err_pos; ++k) {
+            if (R.src[k] > V || R.dst[k] > V) {
+                err_pos = R.arc_pos[k];
+                err = "arc endpoint out of range";
+                found = true;
+                break;
+            }
+        }
+        if (found) break;
+    }
+    if (err_pos != INT64_MAX) {
+        *status = set_error(DPG_ERR_FORMAT, err);
+        return true;
+    }
+    if (np == 0) {
+        *status = set_error(DPG_ERR_FORMAT, "missing 'p' line");
+        return true;
+    }
+    int64_t total = 0;
+    std::vector<int64_t> at(part.size() + 1, 0);
+    for (size_t t = 0; t < part.size(); ++t) at[t + 1] = at[t] + static_cast<int64_t>(part[t].src.size());
+    total = at.back();
+    g->V = static_cast<int32_t>(V);
+    g->source = static_cast<int32_t>(s_val - 1);
+    g->src.resize(static_cast<size_t>(total));
+    g->dst.resize(static_cast<size_t>(total));
+    g->w.resize(static_cast<size_t>(total));
+#pragma omp parallel for num_threads(threads) schedule(static, 1)
+    for (int t = 0; t < static_cast<int>(part.size()); ++t) {
+        const ChunkArcs& R = part[t];
+        for (size_t k = 0; k < R.src.size(); ++k) {
+            g->src[at[t] + k] = R.src[k] - 1;
+            g->dst[at[t] + k] = R.dst[k] - 1;
+            g->w[at[t] + k] = R.w[k];
+        }
+    }
+    g->E = total;
+    if (g->E != declared) {
+        *status = set_error(DPG_ERR_FORMAT, "arc count differs from the 'p' line");
+        return true;
+    }
+    if (g->V > 0 && (g->source < 0 || g->source >= g->V)) {
+        *status = set_error(DPG_ERR_FORMAT, "source vertex out of range");
+        return true;
+    }
+    *status = DPG_OK;
+    return true;
 }
 
 dpg_status read_dimacs10(FILE* fp, ArcList* g) {
@@ -336,18 +522,44 @@ dpg_status dpg_csr_transpose(int32_t V, int64_t E, const int32_t* offsets, const
 }
 
 dpg_status dpg_read_graph(const char* path, int32_t format, dpg_host_graph* out) {
+    return dpg_read_graph_ex(path, format, 0, out);
+}
+
+dpg_status dpg_read_graph_ex(const char* path, int32_t format, int32_t threads, dpg_host_graph* out) {
     if (!path || !out) return set_error(DPG_ERR_INVALID_ARG, "dpg_read_graph: null argument");
+    if (threads < 0) return set_error(DPG_ERR_INVALID_ARG, "threads must be >= 0");
     memset(out, 0, sizeof(*out));
     FILE* fp = fopen(path, "r");
     if (!fp) return set_error(DPG_ERR_IO, std::string("cannot open ") + path);
     FileCloser closer{fp};
     ArcList arcs;
-    dpg_status st;
-    switch (format) {
-        case 0: st = read_dimacs9(fp, &arcs); break;
-        case 1: st = read_dimacs10(fp, &arcs); break;
-        case 2: st = read_slndc(fp, &arcs); break;
-        default: return set_error(DPG_ERR_INVALID_ARG, "Wrong code for dataset");
+    dpg_status st = DPG_OK;
+    bool done = false;
+#ifdef _OPENMP
+    const int nth = threads > 0 ? threads : omp_get_max_threads();
+#else
+    const int nth = 1;
+#endif
+    if (format == 0 && nth > 1 && fseek(fp, 0, SEEK_END) == 0) {
+        // Whole file in memory, then the parallel reader (identical results).
+        const long long n = ftell(fp);
+        if (n > 0 && fseek(fp, 0, SEEK_SET) == 0) {
+            std::vector<char> buf(static_cast<size_t>(n) + 1, 0);
+            if (fread(buf.data(), 1, static_cast<size_t>(n), fp) == static_cast<size_t>(n))
+                done = read_dimacs9_parallel(buf.data(), n, nth, &arcs, &st);
+        }
+        if (!done) {
+            arcs = ArcList();
+            rewind(fp);
+        }
+    }
+    if (!done) {
+        switch (format) {
+            case 0: st = read_dimacs9(fp, &arcs); break;
+            case 1: st = read_dimacs10(fp, &arcs); break;
+            case 2: st = read_slndc(fp, &arcs); break;
+            default: return set_error(DPG_ERR_INVALID_ARG, "Wrong code for dataset");
+        }
     }
     if (st != DPG_OK) return st;
     if (arcs.E > INT32_MAX) return set_error(DPG_ERR_CAPACITY, "more than 2^31-1 arcs");
@@ -365,6 +577,60 @@ dpg_status dpg_read_graph(const char* path, int32_t format, dpg_host_graph* out)
                            out->col, out->weights);
     if (st != DPG_OK) dpg_host_graph_free(out);
     return st;
+}
+
+// Binary CSR cache: "DPGCSR01", int32 V, int64 E, int32 source, int32 has_weights, then offsets
+// [V+1], col [E] and (if present) weights [E], all little-endian int32.
+static const char kCacheMagic[8] = {'D', 'P', 'G', 'C', 'S', 'R', '0', '1'};
+
+dpg_status dpg_write_graph_cache(const char* path, const dpg_host_graph* g) {
+    if (!path || !g || !g->offsets || (g->E > 0 && !g->col)) return set_error(DPG_ERR_INVALID_ARG, "null argument");
+    FILE* fp = fopen(path, "wb");
+    if (!fp) return set_error(DPG_ERR_IO, std::string("cannot open ") + path);
+    FileCloser closer{fp};
+    const int32_t hw = g->weights ? 1 : 0;
+    bool ok = fwrite(kCacheMagic, 1, 8, fp) == 8 && fwrite(&g->V, 4, 1, fp) == 1 && fwrite(&g->E, 8, 1, fp) == 1 &&
+              fwrite(&g->source, 4, 1, fp) == 1 && fwrite(&hw, 4, 1, fp) == 1 &&
+              fwrite(g->offsets, 4, static_cast<size_t>(g->V) + 1, fp) == static_cast<size_t>(g->V) + 1 &&
+              fwrite(g->col, 4, static_cast<size_t>(g->E), fp) == static_cast<size_t>(g->E) &&
+              (!hw || fwrite(g->weights, 4, static_cast<size_t>(g->E), fp) == static_cast<size_t>(g->E));
+    if (!ok) return set_error(DPG_ERR_IO, std::string("write failed: ") + path);
+    return DPG_OK;
+}
+
+dpg_status dpg_read_graph_cache(const char* path, dpg_host_graph* out) {
+    if (!path || !out) return set_error(DPG_ERR_INVALID_ARG, "null argument");
+    memset(out, 0, sizeof(*out));
+    FILE* fp = fopen(path, "rb");
+    if (!fp) return set_error(DPG_ERR_IO, std::string("cannot open ") + path);
+    FileCloser closer{fp};
+    char magic[8];
+    int32_t V = 0, source = 0, hw = 0;
+    int64_t E = 0;
+    if (fread(magic, 1, 8, fp) != 8 || memcmp(magic, kCacheMagic, 8) != 0 || fread(&V, 4, 1, fp) != 1 ||
+        fread(&E, 8, 1, fp) != 1 || fread(&source, 4, 1, fp) != 1 || fread(&hw, 4, 1, fp) != 1 || V < 0 || E < 0 ||
+        E > INT32_MAX || (hw != 0 && hw != 1))
+        return set_error(DPG_ERR_FORMAT, std::string("not a graph cache: ") + path);
+    out->V = V;
+    out->E = E;
+    out->source = source;
+    out->offsets = static_cast<int32_t*>(malloc(4 * (static_cast<size_t>(V) + 1)));
+    out->col = static_cast<int32_t*>(malloc(4 * static_cast<size_t>(E > 0 ? E : 1)));
+    out->weights = static_cast<int32_t*>(malloc(4 * static_cast<size_t>(E > 0 ? E : 1)));
+    if (!out->offsets || !out->col || !out->weights) {
+        dpg_host_graph_free(out);
+        return set_error(DPG_ERR_CAPACITY, "host allocation failed");
+    }
+    bool ok = fread(out->offsets, 4, static_cast<size_t>(V) + 1, fp) == static_cast<size_t>(V) + 1 &&
+              fread(out->col, 4, static_cast<size_t>(E), fp) == static_cast<size_t>(E);
+    if (ok && hw) ok = fread(out->weights, 4, static_cast<size_t>(E), fp) == static_cast<size_t>(E);
+    else if (ok) memset(out->weights, 0, 4 * static_cast<size_t>(E > 0 ? E : 1));
+    if (ok && (out->offsets[0] != 0 || out->offsets[V] != E)) ok = false;
+    if (!ok) {
+        dpg_host_graph_free(out);
+        return set_error(DPG_ERR_FORMAT, std::string("truncated or inconsistent graph cache: ") + path);
+    }
+    return DPG_OK;
 }
 
 void dpg_host_graph_free(dpg_host_graph* g) {

@@ -193,6 +193,12 @@ cudaError_t launch_arc_dot(const SpmmPlanDev& P, const int32_t* col, const float
 cudaError_t launch_gather_values(const float* v, const int32_t* idx, int64_t n, float* out, cudaStream_t s,
                                  int sm_count);
 
+// ---- transposed CSR on the device in invertGraph order (dpg_transpose.cu) ------------------------
+size_t transpose_scratch_bytes(int32_t V, int64_t E);
+cudaError_t launch_transpose(const int32_t* off, const int32_t* col, int32_t V, int64_t E, int32_t* t_off,
+                             int32_t* t_col, int32_t* t_arc, void* scratch, size_t scratch_bytes, cudaStream_t s,
+                             int sm_count);
+
 // ---- recursive BFS with device-side launches (dpg_cdp.cu, relocatable device code) --------------
 struct CdpCounters {
     unsigned long long launches;  // child grids launched

@@ -52,3 +52,26 @@ def test_no_device_is_an_error_not_a_cpu_fallback(tmp_path):
     for app in APPS:
         r = run(app, "-i", p, "-v")
         assert r.returncode == 1 and "DPG_ERR_NO_DEVICE" in r.stdout
+
+
+def test_cache_flag_writes_and_reuses_a_binary_csr(tmp_path):
+    import os
+    import time
+
+    import numpy as np
+
+    rec = load_golden("data_test.json")
+    p = tmp_path / "d.gr"
+    a = rec["arcs"]
+    dpg.write_dimacs9(p, rec["V"], a["src"], a["dst"], a["w"], source=rec["source"])
+    cache = tmp_path / "d.gr.dpgcsr"
+    run("gpu-sssp", "-i", p, "--cache")  # the graph is loaded (and cached) before any device work
+    assert cache.exists()
+    g, h = dpg.read_graph(p), dpg.read_graph_cache(cache)
+    assert np.array_equal(g.offsets, h.offsets) and np.array_equal(g.col, h.col)
+    assert np.array_equal(g.weights, h.weights) and g.source == h.source
+    # A cache older than the input is rebuilt.
+    old = time.time() - 100
+    os.utime(cache, (old, old))
+    run("gpu-sssp", "-i", p, "--cache")
+    assert cache.stat().st_mtime > old + 50
