@@ -52,6 +52,7 @@ def parse_args():
                     help="pagerank is the headline; the others print their own line (used for profiling)")
     ap.add_argument("--scale", type=int, default=0, help="R-MAT scale for --workload spmv/sssp/bfs")
     ap.add_argument("--batch-graphs", type=int, default=512, help="graphs in --workload batch")
+    ap.add_argument("--solution", type=int, default=-1, help="dpg.SOL_* id for --workload sssp/bfs (-1: default)")
     ap.add_argument("--no-relabel", action="store_true", help="turn off the column renaming of SpMV/PageRank")
     return ap.parse_args()
 
@@ -223,15 +224,20 @@ def measure_spmv(dpg, ctx, torch, g, peak, steps, relabel=True):
             "roofline_frac": bytes_spmv / (gather_ms / 1e3) / 1e9 / peak, "bytes_per_launch": bytes_spmv}
 
 
-def measure_expand(dpg, ctx, torch, g, peak, kind, nsrc=4, seed=24):
-    """SSSP or BFS from seeded random sources with out-degree > 0; CUDA events around each solve."""
+def measure_expand(dpg, ctx, torch, g, peak, kind, nsrc=4, seed=24, solution=None):
+    """SSSP or BFS from seeded random sources with out-degree > 0; CUDA events around each solve.
+    solution: a dpg.SOL_* id (None: the library default)."""
     dev = torch.device("cuda", torch.cuda.current_device())
     V, E = g.V, g.E
     dg = dpg.Graph(ctx, g.offsets, g.col, g.weights)
     deg = np.diff(g.offsets)
     srcs = [int(s) for s in np.random.default_rng(seed).choice(np.flatnonzero(deg > 0), nsrc, replace=False)]
     label = torch.empty(V, dtype=torch.int32, device=dev)
-    fn = dpg.sssp_dev if kind == "sssp" else dpg.bfs_dev
+    fn0 = dpg.sssp_dev if kind == "sssp" else dpg.bfs_dev
+    opts = {} if solution is None else {"solution": solution}
+
+    def fn(c, graph, s, ptr):
+        fn0(c, graph, s, ptr, **opts)
     bytes_pass = 4 * (V + 1) + (8 if kind == "sssp" else 4) * E + 8 * V
     ctx.profile(True)
     fn(ctx, dg, srcs[0], label.data_ptr())
@@ -613,7 +619,8 @@ def run_single_workload(args, world=1, rank=0, local=0):
     else:
         scale = args.scale or 24
         g = dpg.rmat_csr(scale, 16, seed=scale, wmin=1, wmax=255)
-        res = measure_expand(dpg, ctx, torch, g, peak, args.workload)
+        res = measure_expand(dpg, ctx, torch, g, peak, args.workload,
+                             solution=None if args.solution < 0 else args.solution)
     if g is None:
         cfg = {"workload": f"batch of {res['graphs']} rmat graphs, V log-uniform [1K, 1M], edge factor "
                            f"{{8, 16, 32}}, {res['sources_per_graph']} SSSP sources + {res['pagerank_sweeps']}-sweep "

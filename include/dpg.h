@@ -61,14 +61,16 @@ typedef enum dpg_solution {
     DPG_SOL_WARP = 2,   /* degree >= threshold: consolidated per warp, expanded by the warp */
     DPG_SOL_BLOCK = 3,  /* degree >= threshold: consolidated per CTA in shared memory, expanded by the CTA */
     DPG_SOL_GRID = 4,   /* degree >= threshold: consolidated grid-wide, expanded by every CTA */
-    DPG_SOL_BINNED = 5  /* warp scan-gather below hub_threshold, grid-wide edge chunks above */
+    DPG_SOL_BINNED = 5, /* warp scan-gather below hub_threshold, grid-wide edge chunks above */
+    DPG_SOL_DIROPT = 6  /* BFS: binned top-down steps, bottom-up steps over in-arcs while the frontier
+                           is large (direction-optimizing); SSSP runs DPG_SOL_BINNED */
 } dpg_solution;
 
 typedef struct dpg_ctx dpg_ctx;
 typedef struct dpg_graph dpg_graph;
 
 typedef struct dpg_expand_opts {
-    int32_t solution;        /* dpg_solution; DPG_SOL_BINNED when the struct pointer is NULL */
+    int32_t solution;        /* dpg_solution; DPG_SOL_DIROPT when the struct pointer is NULL */
     int32_t threshold;       /* consolidation degree threshold; 0 -> DPG_REF_THRESHOLD */
     int32_t hub_threshold;   /* BINNED: degree at which a vertex is expanded grid-wide; 0 -> auto */
     int32_t max_iterations;  /* 0 -> V + 2 (label-correcting never needs more) */

@@ -430,7 +430,7 @@ void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const d
     if (in) *o = *in;
     else {
         memset(o, 0, sizeof(*o));
-        o->solution = DPG_SOL_BINNED;
+        o->solution = DPG_SOL_DIROPT;  // BFS: direction-optimizing; SSSP runs it as DPG_SOL_BINNED
     }
     if (o->threshold <= 0) o->threshold = DPG_REF_THRESHOLD;
     if (o->hub_threshold <= 0) o->hub_threshold = 32;
@@ -450,8 +450,9 @@ dpg_status run_expand(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_
     if (!bfs && !g->weighted) return set_error(DPG_ERR_INVALID_ARG, "SSSP needs a weighted graph");
     dpg_expand_opts o;
     fill_expand_defaults(in_opts, &o, g);
-    if (o.solution < DPG_SOL_THREAD || o.solution > DPG_SOL_BINNED)
+    if (o.solution < DPG_SOL_THREAD || o.solution > DPG_SOL_DIROPT)
         return set_error(DPG_ERR_INVALID_ARG, "unknown solution id");
+    if (!bfs && o.solution == DPG_SOL_DIROPT) o.solution = DPG_SOL_BINNED;  // bottom-up steps are BFS only
     const int32_t min_chunked = (o.solution == DPG_SOL_GRID) ? o.threshold : o.hub_threshold;
     ExpandWorkspace ws;
     dpg_status st = expand_workspace(c, g->V, g->E, min_chunked, &ws);
@@ -472,6 +473,16 @@ dpg_status run_expand(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_
     L.timeout_ns = static_cast<unsigned long long>(o.timeout_seconds * 1e9);
     L.trace = c->trace;
     L.trace_cap = c->trace_cap;
+    if (bfs && o.solution == DPG_SOL_DIROPT) {
+        DPG_TRY(ensure_transpose(const_cast<dpg_graph*>(g)));
+        dpg_status cs = DPG_OK;
+        unsigned long long* cnt = static_cast<unsigned long long*>(arena(c, S_DO_COUNT, 64, &cs));
+        if (cs != DPG_OK) return cs;
+        L.t_off = g->t_off;
+        L.t_col = g->t_col;
+        L.do_mf = cnt;
+        L.do_nf = reinterpret_cast<unsigned*>(cnt + 4);
+    }
     if (c->trace) DPG_CUDA_TRY(cudaMemsetAsync(c->trace, 0, sizeof(unsigned long long) * 4 * c->trace_cap, c->stream));
     c->last_host_iterations = -1;
     DPG_CUDA_TRY(launch_expand(L, ws, c->st, c->stream, c->sm_count, &c->last_grid, &c->last_block, &c->prof));

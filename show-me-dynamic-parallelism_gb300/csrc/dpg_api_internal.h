@@ -34,7 +34,7 @@ enum Slot {
     S_PRG_W, S_PRG_Y, S_PRG_C, S_PRG_V0, S_PRG_V1, S_PRG_V2, S_PRG_V3, S_PRG_PART, S_PRG_RED, S_PRG_FLAGS,
     S_DIRTY0, S_DIRTY1,
     S_CDP_BUF0, S_CDP_BUF1, S_CDP_WORDS,
-    S_TRANSPOSE, S_TRANSPOSE_ARC,
+    S_TRANSPOSE, S_TRANSPOSE_ARC, S_DO_COUNT,
     S_COUNT_SLOTS
 };
 

@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <type_traits>
 
 #include "dpg_kernels.h"
 
@@ -55,6 +56,13 @@ struct ExpandParams {
     // graph; dirty[p][v] = (iteration tag << 32) | mask of the sources whose label of v changed.
     int32_t nsrc;
     unsigned long long* dirty[2];
+    // Direction-optimizing BFS (DPG_SOL_DIROPT): in-arcs, and per rotating parity the out-degree sum
+    // (mf) and the size (nf) of the frontier pushed into it.
+    const int32_t* t_off;
+    const int32_t* t_col;
+    unsigned long long* mf;
+    unsigned* nf;
+    int64_t E;
 };
 
 // Operator interface of the expansion:
@@ -174,6 +182,8 @@ struct PushCtx {
     uint32_t* ccount;
     unsigned long long* dirty;  // MaskSsspOp: marks of the next frontier
     unsigned tag;               // MaskSsspOp: iteration of the next frontier
+    unsigned long long* mf;     // direction-optimizing BFS: out-degree sum of the next frontier
+    unsigned* nf;               // direction-optimizing BFS: size of the next frontier
 };
 
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) {
@@ -212,12 +222,24 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
     bool chunked[U];
     unsigned m[U];
     unsigned cnt = 0;
+    unsigned long long degs = 0;
+    unsigned pushed = 0;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         ok[u] = ok[u] && e[u] > s[u];  // vertices without out-arcs never need expanding
         chunked[u] = kClassify && ok[u] && (e[u] - s[u]) >= P.hub_threshold;
         m[u] = __ballot_sync(kFullMask, ok[u] && !chunked[u]);
         cnt += static_cast<unsigned>(__popc(m[u]));
+        degs += ok[u] ? static_cast<unsigned long long>(e[u] - s[u]) : 0ull;
+        pushed += ok[u] ? 1u : 0u;
+    }
+    if (Q.mf) {  // frontier statistics for the direction choice
+        degs = warp_sum_u64(degs);
+        pushed = static_cast<unsigned>(warp_sum_u64(pushed));
+        if (lane == 0 && pushed) {
+            atomicAdd(Q.mf, degs);
+            atomicAdd(Q.nf, pushed);
+        }
     }
     if (cnt) {
         unsigned base = 0;
@@ -417,7 +439,9 @@ __device__ __forceinline__ void warp_row(const ExpandParams& P, const PushCtx& Q
 template <class Op, int POL, int CH = kHubChunk>
 __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
     using RV = typename Op::RV;
-    constexpr bool kClassify = (POL == DPG_SOL_GRID || POL == DPG_SOL_BINNED);
+    constexpr bool kDirOpt = (POL == DPG_SOL_DIROPT);
+    constexpr bool kBinned = (POL == DPG_SOL_BINNED || kDirOpt);
+    constexpr bool kClassify = (POL == DPG_SOL_GRID || kBinned);
     __shared__ int s_excl[kWarps][32];
     __shared__ int s_start[kWarps][32];
     __shared__ RV s_du[kWarps][32];
@@ -438,6 +462,15 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
     if (threadIdx.x == 0) c_n = 0;
     __syncthreads();
 
+    // Direction-optimizing BFS (Beamer, Asanovic, Patterson, "Direction-Optimizing Breadth-First
+    // Search", SC 2012), with the switch rule set for this kernel: a step runs bottom-up when the
+    // frontier's out-arcs mf exceed both a quarter of the still unexplored arcs and V. A bottom-up
+    // step costs a sweep over all vertices plus in-arc scans, so on GPU it pays only for frontiers
+    // far larger than the CPU rule (mf > unexplored / 14) assumes; measured on R-MAT 22 and 24, this
+    // picks the faster direction at every level. Every CTA reads the same counters after the
+    // barrier, so all make the same choice.
+    bool bottom_up = false;
+    long long unexplored = kDirOpt ? static_cast<long long>(P.E) : 0;
     int j = 0;
     for (;; ++j) {
         const int p = j & 1;
@@ -450,28 +483,61 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
             if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(P.st, DPG_ERR_CAPACITY, 2);
             break;
         }
+        if (kDirOpt) {
+            const unsigned long long mf = *reinterpret_cast<const volatile unsigned long long*>(P.mf + j % 3);
+            const unsigned nf = ld_volatile(P.nf + j % 3);
+            (void)nf;
+            bottom_up = static_cast<long long>(mf) * 4 > unexplored && static_cast<long long>(mf) > P.V;
+            unexplored -= static_cast<long long>(mf);
+        }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             P.ws.qcount[(j + 2) % 3] = 0u;
             P.ws.ccount[(j + 2) % 3] = 0u;
+            if (kDirOpt) {
+                P.mf[(j + 2) % 3] = 0ull;
+                P.nf[(j + 2) % 3] = 0u;
+            }
             if (P.trace && j < P.trace_cap) {
                 P.trace[4 * j + 0] = global_timer_ns();
                 P.trace[4 * j + 1] = n;
                 P.trace[4 * j + 2] = nch;
-                P.trace[4 * j + 3] = 0ull;
+                P.trace[4 * j + 3] = bottom_up ? 2ull : 0ull;
             }
         }
         // Parity selects are written as ternaries so the pointer pairs stay in registers.
         const PushCtx Q = {p ? P.ws.qv[0] : P.ws.qv[1], p ? P.ws.qse[0] : P.ws.qse[1],
                            P.ws.qcount + (j + 1) % 3, p ? P.ws.bmp[0] : P.ws.bmp[1],
                            p ? P.ws.chunks[0] : P.ws.chunks[1], P.ws.ccount + (j + 1) % 3,
-                           p ? P.dirty[0] : P.dirty[1], static_cast<unsigned>(j + 1)};
+                           p ? P.dirty[0] : P.dirty[1], static_cast<unsigned>(j + 1),
+                           kDirOpt ? P.mf + (j + 1) % 3 : nullptr, kDirOpt ? P.nf + (j + 1) % 3 : nullptr};
         const int32_t* qv_cur = p ? P.ws.qv[1] : P.ws.qv[0];
         const int2* qse_cur = p ? P.ws.qse[1] : P.ws.qse[0];
         uint32_t* bmp_cur = p ? P.ws.bmp[1] : P.ws.bmp[0];
         const int4* chunks_cur = p ? P.ws.chunks[1] : P.ws.chunks[0];
         const unsigned fchunks = (n + 31u) / 32u;
 
-        if (POL == DPG_SOL_BLOCK) {
+        if (kDirOpt && bottom_up) {
+            // Bottom-up: every unvisited vertex looks for an in-neighbour on the frontier's level j.
+            for (int64_t base = static_cast<int64_t>(gwarp) * 32; base < P.V; base += static_cast<int64_t>(nwarps) * 32) {
+                const int v = static_cast<int>(base) + lane;
+                bool found = false;
+                if (v < P.V && __ldcg(P.label + v) == DPG_UNDEFINED_LEVEL) {
+                    const int b = __ldg(P.t_off + v), e = __ldg(P.t_off + v + 1);
+                    int k = b;
+                    for (; k < e; ++k)
+                        if (__ldcg(P.label + __ldg(P.t_col + k)) == j) {
+                            found = true;
+                            break;
+                        }
+                    my_edges += static_cast<unsigned long long>((found ? k + 1 : e) - b);
+                    if (found) {
+                        P.label[v] = j + 1;
+                        my_pops += 1;
+                    }
+                }
+                push_converged<Op, kClassify, CH>(P, Q, found, found ? v : 0);
+            }
+        } else if (POL == DPG_SOL_BLOCK) {
             const unsigned per_round = gridDim.x * kWarps;
             const unsigned rounds = (fchunks + per_round - 1) / per_round;
             for (unsigned r = 0; r < rounds; ++r) {
@@ -581,7 +647,7 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                 }
                 if (POL == DPG_SOL_THREAD || POL == DPG_SOL_GRID) {
                     serial_rows<Op, kClassify, CH>(P, Q, has, s, d, du);
-                } else if (POL == DPG_SOL_BINNED) {
+                } else if (kBinned) {
                     warp_gather<Op, kClassify, CH>(P, Q, has, s, d, du, s_excl[warp], s_start[warp], s_du[warp]);
                 } else {
                     const bool big = has && d >= P.threshold;
@@ -648,6 +714,14 @@ __global__ void expand_init_kernel(ExpandParams P, int32_t source, int32_t init_
         P.st->iterations = 0ull;
         P.st->edges = 0ull;
         P.st->pops = 0ull;
+        if (P.mf) {
+            for (int k = 0; k < 3; ++k) {
+                P.mf[k] = 0ull;
+                P.nf[k] = 0u;
+            }
+            P.mf[0] = static_cast<unsigned long long>(e - s);
+            P.nf[0] = e > s ? 1u : 0u;
+        }
         if (chunked) {
             P.ws.ccount[0] = static_cast<unsigned>(nch);
         } else if (e > s) {
@@ -753,6 +827,11 @@ const void* pick_kernel(int solution) {
         case DPG_SOL_BLOCK: return reinterpret_cast<const void*>(expand_kernel<Op, DPG_SOL_BLOCK>);
         case DPG_SOL_GRID: return reinterpret_cast<const void*>(expand_kernel<Op, DPG_SOL_GRID>);
         case DPG_SOL_BINNED: return reinterpret_cast<const void*>(expand_kernel<Op, DPG_SOL_BINNED>);
+        case DPG_SOL_DIROPT:  // bottom-up steps need a level rule: BFS only, SSSP runs binned
+            if constexpr (std::is_same<Op, BfsOp>::value)
+                return reinterpret_cast<const void*>(expand_kernel<BfsOp, DPG_SOL_DIROPT>);
+            else
+                return reinterpret_cast<const void*>(expand_kernel<Op, DPG_SOL_BINNED>);
         default: return nullptr;
     }
 }
@@ -847,7 +926,16 @@ cudaError_t launch_expand(const ExpandLaunch& L, const ExpandWorkspace& ws, DevS
     P.trace = L.trace;
     P.trace_cap = L.trace_cap;
     P.aux = nullptr;
-    const int classify = (L.solution == DPG_SOL_GRID || L.solution == DPG_SOL_BINNED) ? 1 : 0;
+    P.nsrc = 0;
+    P.dirty[0] = P.dirty[1] = nullptr;
+    const bool diropt = L.bfs && L.solution == DPG_SOL_DIROPT;
+    P.t_off = diropt ? L.t_off : nullptr;
+    P.t_col = diropt ? L.t_col : nullptr;
+    P.mf = diropt ? L.do_mf : nullptr;
+    P.nf = diropt ? L.do_nf : nullptr;
+    P.E = L.E;
+    const int classify =
+        (L.solution == DPG_SOL_GRID || L.solution == DPG_SOL_BINNED || L.solution == DPG_SOL_DIROPT) ? 1 : 0;
     const int32_t init_label = L.bfs ? DPG_UNDEFINED_LEVEL : DPG_INF_COST;
     int init_blocks = static_cast<int>((static_cast<int64_t>(L.V) + kBlock - 1) / kBlock);
     if (init_blocks > sm_count * 8) init_blocks = sm_count * 8;

@@ -63,8 +63,13 @@ struct ExpandLaunch {
     int32_t hub_threshold;
     int32_t max_iter;
     unsigned long long timeout_ns;
-    unsigned long long* trace = nullptr;  // nullable: [trace_cap][4] {t_ns, small frontier, chunks, 0}
+    unsigned long long* trace = nullptr;  // nullable: [trace_cap][4] {t_ns, small frontier, chunks, 2 if bottom-up}
     int32_t trace_cap = 0;
+    // Direction-optimizing BFS only: in-arc CSR and the frontier statistics (3 + 3 counters).
+    const int32_t* t_off = nullptr;
+    const int32_t* t_col = nullptr;
+    unsigned long long* do_mf = nullptr;
+    unsigned* do_nf = nullptr;
 };
 
 // Chunk capacity per parity for a graph of V vertices and E arcs when vertices of degree >=

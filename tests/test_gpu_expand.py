@@ -15,7 +15,8 @@ from conftest import dpg, load_golden
 
 pytestmark = pytest.mark.gpu
 
-SOLUTIONS = [dpg.SOL_THREAD, dpg.SOL_NAIVE, dpg.SOL_WARP, dpg.SOL_BLOCK, dpg.SOL_GRID, dpg.SOL_BINNED]
+SOLUTIONS = [dpg.SOL_THREAD, dpg.SOL_NAIVE, dpg.SOL_WARP, dpg.SOL_BLOCK, dpg.SOL_GRID, dpg.SOL_BINNED,
+             dpg.SOL_DIROPT]
 DATA_TEST_DIST = [6853, 8841, 12973, 11908, 5652, 1741, 48923, 0, 16618, 3910, 2320, 61857, 55633, 17426, 19168,
                   10230, 15116, 17185, 16866, 23257]
 DATA_TEST_LEVEL = [3, 4, 4, 3, 2, 1, 2, 0, 1, 2, 1, 4, 3, 2, 3, 3, 4, 5, 5, 4]
@@ -94,7 +95,7 @@ def test_bfs_bit_exact_vs_bfs_cpu(ctx, orc, graphs, devgraphs, name, sol):
 
 
 @pytest.mark.parametrize("threshold,hub", [(1, 1), (2, 32), (16, 64), (64, 256), (1000, 100000)])
-@pytest.mark.parametrize("sol", [dpg.SOL_WARP, dpg.SOL_BLOCK, dpg.SOL_GRID, dpg.SOL_BINNED])
+@pytest.mark.parametrize("sol", [dpg.SOL_WARP, dpg.SOL_BLOCK, dpg.SOL_GRID, dpg.SOL_BINNED, dpg.SOL_DIROPT])
 def test_thresholds(ctx, orc, graphs, devgraphs, threshold, hub, sol):
     g, s = graphs["rmat14"]
     expect = orc.sssp_dijkstra(g.offsets, g.col, g.weights, s)
@@ -242,6 +243,7 @@ def test_sssp_bfs_rmat24_full_size(ctx, orc, rmat24):
         assert ok and reached > g.V // 4
         lv = dpg.bfs(ctx, dg, s)
         assert np.array_equal(lv, orc.bfs_omp(g.offsets, g.col, s))
+        assert np.array_equal(dpg.bfs(ctx, dg, s, solution=dpg.SOL_DIROPT), lv)
     # The reference's consolidation mappings at full size too (one source).
     for sol in (dpg.SOL_WARP, dpg.SOL_BLOCK, dpg.SOL_GRID):
         d2 = dpg.sssp(ctx, dg, sources[0], solution=sol)
@@ -260,3 +262,4 @@ def test_sssp_bfs_grid4096_full_size(ctx):
     lv = dpg.bfs(ctx, dg, s)
     r, c = np.divmod(np.arange(g.V), n)
     assert np.array_equal(lv, np.abs(r - s // n) + np.abs(c - s % n))
+    assert np.array_equal(dpg.bfs(ctx, dg, s, solution=dpg.SOL_DIROPT), lv)
