@@ -47,7 +47,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["dpg", "reference"], default="dpg")
     ap.add_argument("--no-extra", action="store_true", help="skip the SpMV / SSSP / BFS side measurements")
-    ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs", "adjoint", "prgrad", "batch", "cdp"],
+    ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs", "adjoint", "prgrad", "batch", "cdp", "grid"],
                     default="pagerank",
                     help="pagerank is the headline; the others print their own line (used for profiling)")
     ap.add_argument("--scale", type=int, default=0, help="R-MAT scale for --workload spmv/sssp/bfs")
@@ -262,6 +262,8 @@ def measure_expand(dpg, ctx, torch, g, peak, kind, nsrc=4, seed=24, solution=Non
     tr = ctx.trace_read()
     ctx.trace(0)
     trace = [[round((tr[i + 1, 0] - tr[i, 0]) / 1e3, 1), int(tr[i, 1]), int(tr[i, 2])] for i in range(len(tr) - 1)]
+    if len(trace) > 64:  # high-diameter graphs: the first 64 iterations only
+        trace = trace[:64]
     t = statistics.median(times)
     km = statistics.median(kms)
     return {"gteps": E / (t / 1e3) / 1e9, "ms": t, "kernel_ms": km, "trace_us_small_chunks": trace,
@@ -546,6 +548,16 @@ def measure_cdp(dpg, ctx, torch, g, nsrc=3, seed=16):
     return out
 
 
+def measure_grid(dpg, ctx, torch, peak, n=4096, nsrc=2):
+    """The high-diameter graph: an n x n 4-neighbour grid, weights uniform in [1, 1000]. SSSP with the
+    binned and the near-far expansion, and BFS (direction-optimizing)."""
+    g = dpg.grid_csr(n, n, seed=n, wmin=1, wmax=1000)
+    return {f"sssp_grid{n}_binned": measure_expand(dpg, ctx, torch, g, peak, "sssp", nsrc=nsrc, solution=dpg.SOL_BINNED),
+            f"sssp_grid{n}_nearfar": measure_expand(dpg, ctx, torch, g, peak, "sssp", nsrc=nsrc,
+                                                    solution=dpg.SOL_NEARFAR),
+            f"bfs_grid{n}": measure_expand(dpg, ctx, torch, g, peak, "bfs", nsrc=nsrc)}
+
+
 def extra_measurements(dpg, ctx, torch, g, peak, steps):
     """SpMV and the SpMV adjoint on the scale-22 graph; SSSP and BFS on R-MAT scale 24; the PageRank
     edge-weight gradient on scale 20; the 512-graph batch; the recursive CDP2 BFS variants against
@@ -555,6 +567,7 @@ def extra_measurements(dpg, ctx, torch, g, peak, steps):
     g24 = dpg.rmat_csr(24, 16, seed=24, wmin=1, wmax=255)
     out["sssp_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "sssp")
     out["bfs_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "bfs")
+    out.update(measure_grid(dpg, ctx, torch, peak))
     del g24
     g20 = dpg.rmat_csr(20, 16, seed=20, weights=False)
     out["pagerank_grad_rmat20"] = measure_prgrad(dpg, ctx, torch, g20, peak)
@@ -598,6 +611,11 @@ def run_single_workload(args, world=1, rank=0, local=0):
                 return 0
         scale = 0
         g = None
+    elif args.workload == "grid":
+        scale = 0
+        g = dpg.grid_csr(4096, 4096, seed=4096, wmin=1, wmax=1000)
+        res = measure_grid(dpg, ctx, torch, peak)
+        res["gteps"] = res["sssp_grid4096_binned"]["gteps"]
     elif args.workload == "cdp":
         scale = args.scale or 16
         g = dpg.rmat_csr(scale, 16, seed=scale, weights=False)

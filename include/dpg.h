@@ -62,8 +62,10 @@ typedef enum dpg_solution {
     DPG_SOL_BLOCK = 3,  /* degree >= threshold: consolidated per CTA in shared memory, expanded by the CTA */
     DPG_SOL_GRID = 4,   /* degree >= threshold: consolidated grid-wide, expanded by every CTA */
     DPG_SOL_BINNED = 5, /* warp scan-gather below hub_threshold, grid-wide edge chunks above */
-    DPG_SOL_DIROPT = 6  /* BFS: binned top-down steps, bottom-up steps over in-arcs while the frontier
+    DPG_SOL_DIROPT = 6, /* BFS: binned top-down steps, bottom-up steps over in-arcs while the frontier
                            is large (direction-optimizing); SSSP runs DPG_SOL_BINNED */
+    DPG_SOL_NEARFAR = 7 /* SSSP: binned steps over the vertices below a distance threshold, the rest
+                           deferred to a far pile (near-far); BFS runs DPG_SOL_DIROPT */
 } dpg_solution;
 
 typedef struct dpg_ctx dpg_ctx;
@@ -75,6 +77,7 @@ typedef struct dpg_expand_opts {
     int32_t hub_threshold;   /* BINNED: degree at which a vertex is expanded grid-wide; 0 -> auto */
     int32_t max_iterations;  /* 0 -> V + 2 (label-correcting never needs more) */
     double timeout_seconds;  /* limit of each grid-barrier wait; 0 -> 10 s */
+    int32_t delta;           /* NEARFAR: threshold step; 0 -> twice the mean arc weight */
 } dpg_expand_opts;
 
 typedef struct dpg_pr_opts {

@@ -32,7 +32,7 @@ INF_COST = 1073741824  # apps/sssp/src/sssp_wrapper.cu:5
 UNDEFINED_LEVEL = 0x7FFFFFFF  # apps/bfs-rec/src/bfs_rec.h:13
 REF_THRESHOLD = 64  # apps/sssp/src/sssp_kernel.cu:7
 
-SOL_THREAD, SOL_NAIVE, SOL_WARP, SOL_BLOCK, SOL_GRID, SOL_BINNED, SOL_DIROPT = range(7)
+SOL_THREAD, SOL_NAIVE, SOL_WARP, SOL_BLOCK, SOL_GRID, SOL_BINNED, SOL_DIROPT, SOL_NEARFAR = range(8)
 KERNEL_EXPAND, KERNEL_ROWGATHER, KERNEL_FIXUP, KERNEL_INIT = range(4)
 SOLUTION_NAMES = {
     SOL_THREAD: "thread",
@@ -42,6 +42,7 @@ SOLUTION_NAMES = {
     SOL_GRID: "grid",
     SOL_BINNED: "binned",
     SOL_DIROPT: "direction-optimizing (BFS)",
+    SOL_NEARFAR: "near-far (SSSP)",
 }
 
 STATUS = {
@@ -73,6 +74,7 @@ class ExpandOpts(ctypes.Structure):
         ("hub_threshold", c_int32),
         ("max_iterations", c_int32),
         ("timeout_seconds", c_double),
+        ("delta", c_int32),
     ]
 
 
@@ -618,8 +620,9 @@ def rmat_batch(specs, seed: int, wmin=1, wmax=100):
     return out
 
 
-def expand_opts(solution=SOL_DIROPT, threshold=0, hub_threshold=0, max_iterations=0, timeout=0.0) -> ExpandOpts:
-    return ExpandOpts(solution, threshold, hub_threshold, max_iterations, timeout)
+def expand_opts(solution=SOL_DIROPT, threshold=0, hub_threshold=0, max_iterations=0, timeout=0.0,
+                delta=0) -> ExpandOpts:
+    return ExpandOpts(solution, threshold, hub_threshold, max_iterations, timeout, delta)
 
 
 def sssp(ctx: Context, g: Graph, source: int, **opts) -> np.ndarray:

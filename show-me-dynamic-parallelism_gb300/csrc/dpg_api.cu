@@ -72,6 +72,15 @@ dpg_status check_device(dpg_ctx* c) {
     return DPG_OK;
 }
 
+__global__ void weight_sum_kernel(const int32_t* __restrict__ w, int64_t E, unsigned long long* sum) {
+    unsigned long long acc = 0;
+    for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < E;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        acc += static_cast<unsigned long long>(w[e] > 0 ? w[e] : 0);
+    acc = warp_sum_u64(acc);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(sum, acc);
+}
+
 __global__ void validate_interleave_kernel(const int32_t* col, const int32_t* w, int2* adj, int64_t E, int32_t V,
                                            int* bad) {
     for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < E;
@@ -123,11 +132,22 @@ dpg_status graph_finish(dpg_ctx* c, dpg_graph* g, const int32_t* d_w_src) {
         validate_interleave_kernel<<<blocks, 256, 0, c->stream>>>(g->col, d_w_src, g->adj, g->E, g->V, bad);
         DPG_CUDA_TRY(cudaGetLastError());
     }
-    int hbad = 0;
-    DPG_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    unsigned long long* wsum = reinterpret_cast<unsigned long long*>(bad + 2);
+    if (d_w_src && g->E > 0) {
+        DPG_CUDA_TRY(cudaMemsetAsync(wsum, 0, sizeof(unsigned long long), c->stream));
+        weight_sum_kernel<<<c->sm_count * 4, 256, 0, c->stream>>>(d_w_src, g->E, wsum);
+        DPG_CUDA_TRY(cudaGetLastError());
+    }
+    int hbad[4] = {0, 0, 0, 0};
+    DPG_CUDA_TRY(cudaMemcpyAsync(hbad, bad, sizeof(hbad), cudaMemcpyDeviceToHost, c->stream));
     DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-    if (hbad & 1) return set_error(DPG_ERR_INVALID_ARG, "column index out of range");
-    if (hbad & 2) return set_error(DPG_ERR_INVALID_ARG, "weights must be in [0, 2^30)");
+    if (hbad[0] & 1) return set_error(DPG_ERR_INVALID_ARG, "column index out of range");
+    if (hbad[0] & 2) return set_error(DPG_ERR_INVALID_ARG, "weights must be in [0, 2^30)");
+    if (d_w_src && g->E > 0) {
+        unsigned long long sum = 0;
+        memcpy(&sum, hbad + 2, sizeof(sum));
+        g->mean_weight = static_cast<double>(sum) / static_cast<double>(g->E);
+    }
     return DPG_OK;
 }
 
@@ -426,6 +446,9 @@ dpg_status run_color(dpg_ctx* c, dpg_graph* g, const dpg_expand_opts* in_opts, i
     return DPG_OK;
 }
 
+// Near-far threshold step in units of the mean arc weight (see dpg_expand.cu, DPG_SOL_NEARFAR).
+constexpr double kNearFarStep = 2.0;
+
 void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const dpg_graph* g) {
     if (in) *o = *in;
     else {
@@ -450,9 +473,10 @@ dpg_status run_expand(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_
     if (!bfs && !g->weighted) return set_error(DPG_ERR_INVALID_ARG, "SSSP needs a weighted graph");
     dpg_expand_opts o;
     fill_expand_defaults(in_opts, &o, g);
-    if (o.solution < DPG_SOL_THREAD || o.solution > DPG_SOL_DIROPT)
+    if (o.solution < DPG_SOL_THREAD || o.solution > DPG_SOL_NEARFAR)
         return set_error(DPG_ERR_INVALID_ARG, "unknown solution id");
     if (!bfs && o.solution == DPG_SOL_DIROPT) o.solution = DPG_SOL_BINNED;  // bottom-up steps are BFS only
+    if (bfs && o.solution == DPG_SOL_NEARFAR) o.solution = DPG_SOL_DIROPT;  // the threshold is for distances
     const int32_t min_chunked = (o.solution == DPG_SOL_GRID) ? o.threshold : o.hub_threshold;
     ExpandWorkspace ws;
     dpg_status st = expand_workspace(c, g->V, g->E, min_chunked, &ws);
@@ -473,6 +497,21 @@ dpg_status run_expand(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_
     L.timeout_ns = static_cast<unsigned long long>(o.timeout_seconds * 1e9);
     L.trace = c->trace;
     L.trace_cap = c->trace_cap;
+    if (!bfs && o.solution == DPG_SOL_NEARFAR) {
+        // Three piles of E + V {vertex, distance} pairs (at most one current entry per vertex, plus
+        // stale ones; an overflow stops the solve with DPG_ERR_CAPACITY).
+        const int64_t cap = g->E + g->V + 1;
+        dpg_status cs = DPG_OK;
+        for (int k = 0; k < 3; ++k)
+            L.far[k] = static_cast<int2*>(arena(c, static_cast<Slot>(S_FAR0 + k), static_cast<size_t>(cap) * 8, &cs));
+        unsigned* cnt = static_cast<unsigned*>(arena(c, S_FAR_COUNT, 64, &cs));
+        if (cs != DPG_OK) return cs;
+        L.far_count = cnt;
+        L.far_min = reinterpret_cast<int*>(cnt + 4);
+        L.far_cap = cap;
+        const double mw = g->mean_weight > 0 ? g->mean_weight : 1.0;
+        L.delta = o.delta > 0 ? o.delta : static_cast<int32_t>(std::max(1.0, std::min(1e9, kNearFarStep * mw)));
+    }
     if (bfs && o.solution == DPG_SOL_DIROPT) {
         DPG_TRY(ensure_transpose(const_cast<dpg_graph*>(g)));
         dpg_status cs = DPG_OK;

@@ -34,7 +34,7 @@ enum Slot {
     S_PRG_W, S_PRG_Y, S_PRG_C, S_PRG_V0, S_PRG_V1, S_PRG_V2, S_PRG_V3, S_PRG_PART, S_PRG_RED, S_PRG_FLAGS,
     S_DIRTY0, S_DIRTY1,
     S_CDP_BUF0, S_CDP_BUF1, S_CDP_WORDS,
-    S_TRANSPOSE, S_TRANSPOSE_ARC, S_DO_COUNT,
+    S_TRANSPOSE, S_TRANSPOSE_ARC, S_DO_COUNT, S_FAR0, S_FAR1, S_FAR2, S_FAR_COUNT,
     S_COUNT_SLOTS
 };
 
@@ -143,6 +143,7 @@ struct dpg_graph {
     int2* adj = nullptr;
     std::vector<int32_t> h_off;
     int32_t max_degree = 0;
+    double mean_weight = 0.0;  // weighted graphs: mean arc weight (the near-far step default)
     bool plan_ready = false;
     RowPlanDev plan;
     // Column renaming by frequency for the row gathers (dpg_layout.cu); built on first use.

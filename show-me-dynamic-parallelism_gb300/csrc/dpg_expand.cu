@@ -63,6 +63,12 @@ struct ExpandParams {
     unsigned long long* mf;
     unsigned* nf;
     int64_t E;
+    // Near-far SSSP (DPG_SOL_NEARFAR): three rotating piles of deferred {vertex, distance} pairs.
+    int2* far[3];
+    unsigned* far_count;  // [3]
+    int* far_min;         // [3] smallest distance pushed into each pile
+    int64_t far_cap;
+    int32_t delta;
 };
 
 // Operator interface of the expansion:
@@ -184,6 +190,10 @@ struct PushCtx {
     unsigned tag;               // MaskSsspOp: iteration of the next frontier
     unsigned long long* mf;     // direction-optimizing BFS: out-degree sum of the next frontier
     unsigned* nf;               // direction-optimizing BFS: size of the next frontier
+    int2* far;                  // near-far SSSP: pile receiving distances >= threshold (null: off)
+    unsigned* far_count;
+    int* far_min;
+    int threshold;
 };
 
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) {
@@ -292,6 +302,41 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
     }
 }
 
+// Near-far: appends the slots with ok[u] to the far pile as {vertex, distance} (warp-aggregated),
+// and lowers the pile's minimum distance.
+template <int U>
+__device__ __forceinline__ void far_push(const ExpandParams& P, const PushCtx& Q, const bool (&ok)[U],
+                                         const int (&v)[U], const int (&c)[U]) {
+    const int lane = lane_id();
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned m[U];
+    unsigned cnt = 0;
+    int cmin = 0x7FFFFFFF;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        m[u] = __ballot_sync(kFullMask, ok[u]);
+        cnt += static_cast<unsigned>(__popc(m[u]));
+        if (ok[u]) cmin = min(cmin, c[u]);
+    }
+    if (cnt == 0) return;
+    cmin = __reduce_min_sync(kFullMask, cmin);
+    unsigned base = 0;
+    if (lane == 0) {
+        base = atomicAdd(Q.far_count, cnt);
+        atomicMin(Q.far_min, cmin);
+    }
+    base = __shfl_sync(kFullMask, base, 0);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (ok[u]) {
+            const unsigned pos = base + static_cast<unsigned>(__popc(m[u] & lt));
+            if (static_cast<int64_t>(pos) < P.far_cap) __stcg(Q.far + pos, make_int2(v[u], c[u]));
+            else raise_error(P.st, DPG_ERR_CAPACITY, 14);
+        }
+        base += static_cast<unsigned>(__popc(m[u]));
+    }
+}
+
 // U independent relaxations per lane, issued phase by phase (U adjacency loads, U label loads, U
 // atomics, one batched push) so each warp keeps U memory operations in flight instead of one.
 template <class Op, bool kClassify, int CH, int U>
@@ -342,6 +387,15 @@ __device__ __forceinline__ void relax_batch(const ExpandParams& P, const PushCtx
 #pragma unroll
         for (int u = 0; u < U; ++u)
             ok[u] = act[u] && Op::want(v[u], cand[u], cur[u]) && Op::commit(P, v[u], cand[u]);
+        if (Q.far) {  // near-far: improvements at or above the threshold wait in the far pile
+            bool far[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                far[u] = ok[u] && cand[u] >= Q.threshold;
+                ok[u] = ok[u] && !far[u];
+            }
+            far_push<U>(P, Q, far, v, cand);
+        }
     }
     push_batch<Op, kClassify, CH, U>(P, Q, ok, v, row);
 }
@@ -440,7 +494,8 @@ template <class Op, int POL, int CH = kHubChunk>
 __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
     using RV = typename Op::RV;
     constexpr bool kDirOpt = (POL == DPG_SOL_DIROPT);
-    constexpr bool kBinned = (POL == DPG_SOL_BINNED || kDirOpt);
+    constexpr bool kNearFar = (POL == DPG_SOL_NEARFAR);
+    constexpr bool kBinned = (POL == DPG_SOL_BINNED || kDirOpt || kNearFar);
     constexpr bool kClassify = (POL == DPG_SOL_GRID || kBinned);
     __shared__ int s_excl[kWarps][32];
     __shared__ int s_start[kWarps][32];
@@ -471,6 +526,14 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
     // barrier, so all make the same choice.
     bool bottom_up = false;
     long long unexplored = kDirOpt ? static_cast<long long>(P.E) : 0;
+    // Near-far (Davidson, Baxter, Garland, Owens, "Work-Efficient Parallel GPU Methods for
+    // Single-Source Shortest Paths", IPDPS 2014): improvements below the threshold form the next
+    // frontier, the others wait in the active far pile. When the frontier runs dry the threshold
+    // moves past delta and the pile's minimum, and one split step moves the pile's still-current
+    // entries below it into the frontier and the rest into the next pile. Piles rotate over three
+    // buffers so the one being reset is never the one being read or written.
+    int threshold = kNearFar ? P.delta : 0;
+    int pile = 0;
     int j = 0;
     for (;; ++j) {
         const int p = j & 1;
@@ -478,7 +541,17 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
         // (which stops the loop at the barrier); the clamps keep every read inside its buffer anyway.
         const unsigned n = min(ld_volatile(P.ws.qcount + (j % 3)), static_cast<unsigned>(P.ws.cap_v));
         const unsigned nch = min(ld_volatile(P.ws.ccount + (j % 3)), static_cast<unsigned>(P.ws.cap_chunks));
-        if (n == 0 && nch == 0) break;
+        bool split = false;
+        unsigned far_n = 0;
+        if (kNearFar && n == 0 && nch == 0) {
+            far_n = static_cast<unsigned>(min(static_cast<int64_t>(ld_volatile(P.far_count + pile)), P.far_cap));
+            if (far_n == 0) break;
+            split = true;
+            const int fmin = *reinterpret_cast<const volatile int*>(P.far_min + pile);
+            const long long t = max(static_cast<long long>(threshold) + P.delta, static_cast<long long>(fmin) + 1);
+            threshold = static_cast<int>(min(t, static_cast<long long>(0x7FFFFFFF)));
+        }
+        if (!split && n == 0 && nch == 0) break;
         if (j >= P.max_iter) {
             if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(P.st, DPG_ERR_CAPACITY, 2);
             break;
@@ -497,6 +570,10 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                 P.mf[(j + 2) % 3] = 0ull;
                 P.nf[(j + 2) % 3] = 0u;
             }
+            if (kNearFar && split) {  // the pile read by the previous split is free again
+                P.far_count[(pile + 2) % 3] = 0u;
+                P.far_min[(pile + 2) % 3] = 0x7FFFFFFF;
+            }
             if (P.trace && j < P.trace_cap) {
                 P.trace[4 * j + 0] = global_timer_ns();
                 P.trace[4 * j + 1] = n;
@@ -509,14 +586,35 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
                            P.ws.qcount + (j + 1) % 3, p ? P.ws.bmp[0] : P.ws.bmp[1],
                            p ? P.ws.chunks[0] : P.ws.chunks[1], P.ws.ccount + (j + 1) % 3,
                            p ? P.dirty[0] : P.dirty[1], static_cast<unsigned>(j + 1),
-                           kDirOpt ? P.mf + (j + 1) % 3 : nullptr, kDirOpt ? P.nf + (j + 1) % 3 : nullptr};
+                           kDirOpt ? P.mf + (j + 1) % 3 : nullptr, kDirOpt ? P.nf + (j + 1) % 3 : nullptr,
+                           kNearFar ? P.far[split ? (pile + 1) % 3 : pile] : nullptr,
+                           kNearFar ? P.far_count + (split ? (pile + 1) % 3 : pile) : nullptr,
+                           kNearFar ? P.far_min + (split ? (pile + 1) % 3 : pile) : nullptr, threshold};
         const int32_t* qv_cur = p ? P.ws.qv[1] : P.ws.qv[0];
         const int2* qse_cur = p ? P.ws.qse[1] : P.ws.qse[0];
         uint32_t* bmp_cur = p ? P.ws.bmp[1] : P.ws.bmp[0];
         const int4* chunks_cur = p ? P.ws.chunks[1] : P.ws.chunks[0];
         const unsigned fchunks = (n + 31u) / 32u;
 
-        if (kDirOpt && bottom_up) {
+        if (kNearFar && split) {
+            // Split: still-current entries below the new threshold join the frontier (de-duplicated
+            // by the bitmap), the rest move to the next pile; stale entries are dropped.
+            const int2* src = P.far[pile];
+            for (int64_t base = static_cast<int64_t>(gwarp) * 32; base < far_n; base += static_cast<int64_t>(nwarps) * 32) {
+                const int64_t i = base + lane;
+                int2 F = make_int2(0, 0);
+                bool cur = false;
+                if (i < far_n) {
+                    F = __ldcg(src + i);
+                    cur = __ldcg(P.label + F.x) == F.y;
+                }
+                bool keep[1] = {cur && F.y >= threshold};
+                const int fv[1] = {F.x};
+                const int fc[1] = {F.y};
+                far_push<1>(P, Q, keep, fv, fc);
+                push_converged<Op, kClassify, CH>(P, Q, cur && F.y < threshold, cur ? F.x : 0);
+            }
+        } else if (kDirOpt && bottom_up) {
             // Bottom-up: every unvisited vertex looks for an in-neighbour on the frontier's level j.
             for (int64_t base = static_cast<int64_t>(gwarp) * 32; base < P.V; base += static_cast<int64_t>(nwarps) * 32) {
                 const int v = static_cast<int>(base) + lane;
@@ -669,6 +767,7 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
             }
         }
         if (!grid_barrier(P.st, gridDim.x, P.timeout_ns)) break;
+        if (kNearFar && split) pile = (pile + 1) % 3;
     }
 
     my_edges = warp_sum_u64(my_edges);
@@ -714,6 +813,12 @@ __global__ void expand_init_kernel(ExpandParams P, int32_t source, int32_t init_
         P.st->iterations = 0ull;
         P.st->edges = 0ull;
         P.st->pops = 0ull;
+        if (P.far_count) {
+            for (int k = 0; k < 3; ++k) {
+                P.far_count[k] = 0u;
+                P.far_min[k] = 0x7FFFFFFF;
+            }
+        }
         if (P.mf) {
             for (int k = 0; k < 3; ++k) {
                 P.mf[k] = 0ull;
@@ -827,6 +932,11 @@ const void* pick_kernel(int solution) {
         case DPG_SOL_BLOCK: return reinterpret_cast<const void*>(expand_kernel<Op, DPG_SOL_BLOCK>);
         case DPG_SOL_GRID: return reinterpret_cast<const void*>(expand_kernel<Op, DPG_SOL_GRID>);
         case DPG_SOL_BINNED: return reinterpret_cast<const void*>(expand_kernel<Op, DPG_SOL_BINNED>);
+        case DPG_SOL_NEARFAR:  // a distance threshold: SSSP only, BFS runs direction-optimizing
+            if constexpr (std::is_same<Op, SsspOp>::value)
+                return reinterpret_cast<const void*>(expand_kernel<SsspOp, DPG_SOL_NEARFAR>);
+            else
+                return reinterpret_cast<const void*>(expand_kernel<BfsOp, DPG_SOL_DIROPT>);
         case DPG_SOL_DIROPT:  // bottom-up steps need a level rule: BFS only, SSSP runs binned
             if constexpr (std::is_same<Op, BfsOp>::value)
                 return reinterpret_cast<const void*>(expand_kernel<BfsOp, DPG_SOL_DIROPT>);
@@ -928,14 +1038,21 @@ cudaError_t launch_expand(const ExpandLaunch& L, const ExpandWorkspace& ws, DevS
     P.aux = nullptr;
     P.nsrc = 0;
     P.dirty[0] = P.dirty[1] = nullptr;
-    const bool diropt = L.bfs && L.solution == DPG_SOL_DIROPT;
+    const bool diropt = L.bfs && (L.solution == DPG_SOL_DIROPT || L.solution == DPG_SOL_NEARFAR);
+    const bool nearfar = !L.bfs && L.solution == DPG_SOL_NEARFAR;
+    for (int k = 0; k < 3; ++k) P.far[k] = nearfar ? L.far[k] : nullptr;
+    P.far_count = nearfar ? L.far_count : nullptr;
+    P.far_min = nearfar ? L.far_min : nullptr;
+    P.far_cap = L.far_cap;
+    P.delta = L.delta > 0 ? L.delta : 1;
     P.t_off = diropt ? L.t_off : nullptr;
     P.t_col = diropt ? L.t_col : nullptr;
     P.mf = diropt ? L.do_mf : nullptr;
     P.nf = diropt ? L.do_nf : nullptr;
     P.E = L.E;
     const int classify =
-        (L.solution == DPG_SOL_GRID || L.solution == DPG_SOL_BINNED || L.solution == DPG_SOL_DIROPT) ? 1 : 0;
+        (L.solution == DPG_SOL_GRID || L.solution == DPG_SOL_BINNED || L.solution == DPG_SOL_DIROPT ||
+         L.solution == DPG_SOL_NEARFAR) ? 1 : 0;
     const int32_t init_label = L.bfs ? DPG_UNDEFINED_LEVEL : DPG_INF_COST;
     int init_blocks = static_cast<int>((static_cast<int64_t>(L.V) + kBlock - 1) / kBlock);
     if (init_blocks > sm_count * 8) init_blocks = sm_count * 8;

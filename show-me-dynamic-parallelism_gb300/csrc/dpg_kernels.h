@@ -70,6 +70,12 @@ struct ExpandLaunch {
     const int32_t* t_col = nullptr;
     unsigned long long* do_mf = nullptr;
     unsigned* do_nf = nullptr;
+    // Near-far SSSP only: three piles of far_cap {vertex, distance} pairs, 3 counts, 3 minima.
+    int2* far[3] = {nullptr, nullptr, nullptr};
+    unsigned* far_count = nullptr;
+    int* far_min = nullptr;
+    int64_t far_cap = 0;
+    int32_t delta = 0;
 };
 
 // Chunk capacity per parity for a graph of V vertices and E arcs when vertices of degree >=

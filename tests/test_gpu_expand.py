@@ -16,7 +16,7 @@ from conftest import dpg, load_golden
 pytestmark = pytest.mark.gpu
 
 SOLUTIONS = [dpg.SOL_THREAD, dpg.SOL_NAIVE, dpg.SOL_WARP, dpg.SOL_BLOCK, dpg.SOL_GRID, dpg.SOL_BINNED,
-             dpg.SOL_DIROPT]
+             dpg.SOL_DIROPT, dpg.SOL_NEARFAR]
 DATA_TEST_DIST = [6853, 8841, 12973, 11908, 5652, 1741, 48923, 0, 16618, 3910, 2320, 61857, 55633, 17426, 19168,
                   10230, 15116, 17185, 16866, 23257]
 DATA_TEST_LEVEL = [3, 4, 4, 3, 2, 1, 2, 0, 1, 2, 1, 4, 3, 2, 3, 3, 4, 5, 5, 4]
@@ -95,7 +95,8 @@ def test_bfs_bit_exact_vs_bfs_cpu(ctx, orc, graphs, devgraphs, name, sol):
 
 
 @pytest.mark.parametrize("threshold,hub", [(1, 1), (2, 32), (16, 64), (64, 256), (1000, 100000)])
-@pytest.mark.parametrize("sol", [dpg.SOL_WARP, dpg.SOL_BLOCK, dpg.SOL_GRID, dpg.SOL_BINNED, dpg.SOL_DIROPT])
+@pytest.mark.parametrize("sol", [dpg.SOL_WARP, dpg.SOL_BLOCK, dpg.SOL_GRID, dpg.SOL_BINNED, dpg.SOL_DIROPT,
+                                 dpg.SOL_NEARFAR])
 def test_thresholds(ctx, orc, graphs, devgraphs, threshold, hub, sol):
     g, s = graphs["rmat14"]
     expect = orc.sssp_dijkstra(g.offsets, g.col, g.weights, s)
@@ -244,8 +245,8 @@ def test_sssp_bfs_rmat24_full_size(ctx, orc, rmat24):
         lv = dpg.bfs(ctx, dg, s)
         assert np.array_equal(lv, orc.bfs_omp(g.offsets, g.col, s))
         assert np.array_equal(dpg.bfs(ctx, dg, s, solution=dpg.SOL_DIROPT), lv)
-    # The reference's consolidation mappings at full size too (one source).
-    for sol in (dpg.SOL_WARP, dpg.SOL_BLOCK, dpg.SOL_GRID):
+    # The reference's consolidation mappings and near-far at full size too (one source).
+    for sol in (dpg.SOL_WARP, dpg.SOL_BLOCK, dpg.SOL_GRID, dpg.SOL_NEARFAR):
         d2 = dpg.sssp(ctx, dg, sources[0], solution=sol)
         assert np.array_equal(d2, dpg.sssp(ctx, dg, sources[0]))
 
@@ -259,7 +260,22 @@ def test_sssp_bfs_grid4096_full_size(ctx):
     dist = dpg.sssp(ctx, dg, s)
     ok, reached = _certificate(g.offsets, g.col, g.weights, dist, s)
     assert ok and reached == g.V
+    assert np.array_equal(dpg.sssp(ctx, dg, s, solution=dpg.SOL_NEARFAR), dist)
     lv = dpg.bfs(ctx, dg, s)
     r, c = np.divmod(np.arange(g.V), n)
     assert np.array_equal(lv, np.abs(r - s // n) + np.abs(c - s % n))
     assert np.array_equal(dpg.bfs(ctx, dg, s, solution=dpg.SOL_DIROPT), lv)
+
+
+@pytest.mark.parametrize("delta", [1, 7, 100, 10**9])
+def test_nearfar_any_step_gives_exact_distances(ctx, orc, delta):
+    g = dpg.rmat_csr(12, 16, seed=12, wmin=1, wmax=255)
+    dg = dpg.Graph(ctx, g.offsets, g.col, g.weights)
+    s = int(np.argmax(np.diff(g.offsets)))
+    exact = orc.sssp_dijkstra(g.offsets, g.col, g.weights, s)
+    assert np.array_equal(dpg.sssp(ctx, dg, s, solution=dpg.SOL_NEARFAR, delta=delta), exact)
+    # Zero-weight arcs and distances landing exactly on a threshold.
+    z = dpg.csr_from_arcs(6, [0, 1, 2, 3, 4, 0], [1, 2, 3, 4, 5, 5], [0, delta % 1000, 0, 0, delta % 1000, 999])
+    dz = dpg.Graph(ctx, z.offsets, z.col, z.weights)
+    assert np.array_equal(dpg.sssp(ctx, dz, 0, solution=dpg.SOL_NEARFAR, delta=delta),
+                          orc.sssp_dijkstra(z.offsets, z.col, z.weights, 0))
