@@ -436,7 +436,7 @@ def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=51
         od = torch.from_numpy(np.diff(g.offsets).astype(np.int32)).to(dev)
         plain.append((dpg.Graph(ctx, g.offsets, g.col, g.weights), dpg.Graph(ctx, in_off, in_col), od))
     pdist = torch.empty(nsrc * V, dtype=torch.int32, device=dev)
-    prank_v = torch.empty(V, dtype=torch.float32, device=dev)
+    prank = torch.empty(V, dtype=torch.float32, device=dev)
 
     def loop():
         for k, (go, gi, od) in enumerate(plain):
