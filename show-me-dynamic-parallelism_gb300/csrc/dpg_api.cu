@@ -39,6 +39,22 @@ dpg_status use_device(dpg_ctx* c) {
     return DPG_OK;
 }
 
+#ifndef DPG_GRAPH_POOL
+#define DPG_GRAPH_POOL 1
+#endif
+
+cudaError_t dev_alloc(dpg_ctx* c, void** p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (DPG_GRAPH_POOL && c && c->pool) return cudaMallocFromPoolAsync(p, bytes, c->pool, c->stream);
+    return cudaMalloc(p, bytes);
+}
+
+void dev_free(dpg_ctx* c, void* p) {
+    if (!p) return;
+    if (DPG_GRAPH_POOL && c && c->pool) cudaFreeAsync(p, c->stream);
+    else cudaFree(p);
+}
+
 void* arena(dpg_ctx* c, Slot s, size_t bytes, dpg_status* status) {
     Buf& b = c->bufs[s];
     if (bytes == 0) bytes = 16;
@@ -158,29 +174,29 @@ void graph_free_device(dpg_graph* g) {
         delete g->tgraph;
         g->tgraph = nullptr;
     }
-    cudaFree(g->off);
-    cudaFree(g->col);
-    cudaFree(g->adj);
-    cudaFree(g->perm);
-    cudaFree(g->inv);
-    cudaFree(g->pcol);
-    cudaFree(g->t_off);
-    cudaFree(g->t_col);
+    dev_free(g->ctx, g->off);
+    dev_free(g->ctx, g->col);
+    dev_free(g->ctx, g->adj);
+    dev_free(g->ctx, g->perm);
+    dev_free(g->ctx, g->inv);
+    dev_free(g->ctx, g->pcol);
+    dev_free(g->ctx, g->t_off);
+    dev_free(g->ctx, g->t_col);
     g->perm = g->inv = g->pcol = g->t_off = g->t_col = nullptr;
     for (SpmmPlanDev* p : {&g->spmm_plan, &g->spmm_t_plan}) {
-        cudaFree(p->items);
-        cudaFree(p->hubs);
+        dev_free(g->ctx, p->items);
+        dev_free(g->ctx, p->hubs);
         *p = SpmmPlanDev();
     }
-    cudaFree(g->tt_col);
-    cudaFree(g->tt_arc);
+    dev_free(g->ctx, g->tt_col);
+    dev_free(g->ctx, g->tt_arc);
     g->tt_col = g->tt_arc = nullptr;
     g->spmm_ready = g->spmm_t_ready = false;
     g->relabel_ready = false;
-    cudaFree(g->plan.tiles);
-    cudaFree(g->plan.lane_r0);
-    cudaFree(g->plan.hubs_small);
-    cudaFree(g->plan.hubs_big);
+    dev_free(g->ctx, g->plan.tiles);
+    dev_free(g->ctx, g->plan.lane_r0);
+    dev_free(g->ctx, g->plan.hubs_small);
+    dev_free(g->ctx, g->plan.hubs_big);
     g->off = nullptr;
     g->col = nullptr;
     g->adj = nullptr;
@@ -197,10 +213,11 @@ dpg_status ensure_plan(dpg_graph* g) {
     d.nhub_big = static_cast<int32_t>(hp.hubs_big.size());
     d.nseg = hp.nseg;
     cudaStream_t s = g->ctx->stream;
-    DPG_CUDA_TRY(cudaMalloc(&d.tiles, sizeof(int4) * (hp.tiles.size() + 1)));
-    DPG_CUDA_TRY(cudaMalloc(&d.lane_r0, 32 * (hp.tiles.size() + 1)));
-    DPG_CUDA_TRY(cudaMalloc(&d.hubs_small, sizeof(int4) * (hp.hubs_small.size() + 1)));
-    DPG_CUDA_TRY(cudaMalloc(&d.hubs_big, sizeof(int4) * (hp.hubs_big.size() + 1)));
+    dpg_ctx* c = g->ctx;
+    DPG_CUDA_TRY(dev_alloc(c, &d.tiles, sizeof(int4) * (hp.tiles.size() + 1)));
+    DPG_CUDA_TRY(dev_alloc(c, &d.lane_r0, 32 * (hp.tiles.size() + 1)));
+    DPG_CUDA_TRY(dev_alloc(c, &d.hubs_small, sizeof(int4) * (hp.hubs_small.size() + 1)));
+    DPG_CUDA_TRY(dev_alloc(c, &d.hubs_big, sizeof(int4) * (hp.hubs_big.size() + 1)));
     if (!hp.tiles.empty())
         DPG_CUDA_TRY(cudaMemcpyAsync(d.tiles, hp.tiles.data(), sizeof(int4) * hp.tiles.size(), cudaMemcpyHostToDevice, s));
     if (!hp.hubs_small.empty())
@@ -235,19 +252,18 @@ dpg_status ensure_relabel(dpg_graph* g) {
     const size_t nv = static_cast<size_t>(g->V);
     const std::vector<int32_t>& seg = g->relabel_segments;
     int32_t* counts = nullptr;
-    DPG_CUDA_TRY(cudaMalloc(&counts, nv * 4));
-    cudaError_t e = cudaMalloc(&g->perm, nv * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&g->inv, nv * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&g->pcol, static_cast<size_t>(g->E > 0 ? g->E : 1) * 4);
+    DPG_CUDA_TRY(dev_alloc(c, &counts, nv * 4));
+    cudaError_t e = dev_alloc(c, &g->perm, nv * 4);
+    if (e == cudaSuccess) e = dev_alloc(c, &g->inv, nv * 4);
+    if (e == cudaSuccess) e = dev_alloc(c, &g->pcol, static_cast<size_t>(g->E > 0 ? g->E : 1) * 4);
     if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, nv * 4, c->stream);
     if (e == cudaSuccess) e = launch_column_histogram(g->col, g->E, counts, c->stream, c->sm_count);
     if (e == cudaSuccess && seg.size() < 2) {
         // One graph: the whole order on the device.
         int32_t* scratch = nullptr;
-        e = cudaMalloc(&scratch, frequency_order_scratch_bytes(g->V));
+        e = dev_alloc(c, &scratch, frequency_order_scratch_bytes(g->V));
         if (e == cudaSuccess) e = launch_frequency_order(counts, g->V, scratch, g->perm, g->inv, c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-        cudaFree(scratch);
+        dev_free(c, scratch);
     } else if (e == cudaSuccess) {
         // Packed graphs: each segment ordered on its own, on the host.
         std::vector<int32_t> h_counts(nv), h_perm(nv), h_inv(nv);
@@ -269,13 +285,13 @@ dpg_status ensure_relabel(dpg_graph* g) {
             if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         }
     }
-    cudaFree(counts);
     if (e == cudaSuccess) e = launch_relabel_columns(g->col, g->perm, g->E, g->pcol, c->stream, c->sm_count);
+    dev_free(c, counts);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
-        cudaFree(g->perm);
-        cudaFree(g->inv);
-        cudaFree(g->pcol);
+        dev_free(c, g->perm);
+        dev_free(c, g->inv);
+        dev_free(c, g->pcol);
         g->perm = g->inv = g->pcol = nullptr;
         return set_error(DPG_ERR_CUDA, std::string("column renaming: ") + cudaGetErrorString(e));
     }
@@ -287,8 +303,8 @@ dpg_status upload_spmm_plan(dpg_ctx* c, const SpmmPlanHost& hp, SpmmPlanDev* d) 
     d->nitems = static_cast<int32_t>(hp.items.size());
     d->nhubs = static_cast<int32_t>(hp.hubs.size());
     d->nseg = hp.nseg;
-    DPG_CUDA_TRY(cudaMalloc(&d->items, sizeof(int4) * (hp.items.size() + 1)));
-    DPG_CUDA_TRY(cudaMalloc(&d->hubs, sizeof(int4) * (hp.hubs.size() + 1)));
+    DPG_CUDA_TRY(dev_alloc(c, &d->items, sizeof(int4) * (hp.items.size() + 1)));
+    DPG_CUDA_TRY(dev_alloc(c, &d->hubs, sizeof(int4) * (hp.hubs.size() + 1)));
     if (!hp.items.empty())
         DPG_CUDA_TRY(cudaMemcpyAsync(d->items, hp.items.data(), sizeof(int4) * hp.items.size(), cudaMemcpyHostToDevice,
                                      c->stream));
@@ -316,10 +332,10 @@ dpg_status ensure_spmm_transpose(dpg_graph* g, bool need_graph = false) {
     dpg_ctx* c = g->ctx;
     const size_t nv = static_cast<size_t>(g->V), ne = static_cast<size_t>(g->E > 0 ? g->E : 1);
     int32_t* t_off = nullptr;
-    DPG_CUDA_TRY(cudaMalloc(&t_off, (nv + 1) * 4));
+    DPG_CUDA_TRY(dev_alloc(c, &t_off, (nv + 1) * 4));
     cudaError_t e = cudaSuccess;
-    if (!g->tt_col) e = cudaMalloc(&g->tt_col, ne * 4);
-    if (e == cudaSuccess && !g->tt_arc) e = cudaMalloc(&g->tt_arc, ne * 4);
+    if (!g->tt_col) e = dev_alloc(c, &g->tt_col, ne * 4);
+    if (e == cudaSuccess && !g->tt_arc) e = dev_alloc(c, &g->tt_arc, ne * 4);
     dpg_status st = DPG_OK;
     const size_t scratch_bytes = transpose_scratch_bytes(g->V, g->E);
     void* scratch = e == cudaSuccess ? arena(c, S_TRANSPOSE, scratch_bytes, &st) : nullptr;
@@ -331,7 +347,7 @@ dpg_status ensure_spmm_transpose(dpg_graph* g, bool need_graph = false) {
         e = cudaMemcpyAsync(h_t_off.data(), t_off, (nv + 1) * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && st == DPG_OK) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess || st != DPG_OK) {
-        cudaFree(t_off);
+        dev_free(c, t_off);
         return st != DPG_OK ? st : set_error(DPG_ERR_CUDA, std::string("device transpose: ") + cudaGetErrorString(e));
     }
     if (!g->spmm_t_ready) {
@@ -344,7 +360,7 @@ dpg_status ensure_spmm_transpose(dpg_graph* g, bool need_graph = false) {
         st = graph_create_common(c, g->V, g->E, t_off, g->tt_col, nullptr, true, &g->tgraph);
         if (st == DPG_OK) g->tgraph->relabel = g->relabel;
     }
-    cudaFree(t_off);
+    dev_free(c, t_off);
     return st;
 }
 
@@ -383,14 +399,14 @@ dpg_status ensure_transpose(dpg_graph* g) {
     dpg_ctx* c = g->ctx;
     const size_t nv = static_cast<size_t>(g->V);
     int32_t* cursor = nullptr;
-    DPG_CUDA_TRY(cudaMalloc(&cursor, (nv + 1) * 4));
+    DPG_CUDA_TRY(dev_alloc(c, &cursor, (nv + 1) * 4));
     std::vector<int32_t> h(nv + 1, 0);
     cudaError_t e = cudaMemsetAsync(cursor, 0, (nv + 1) * 4, c->stream);
     if (e == cudaSuccess) e = launch_column_histogram(g->col, g->E, cursor, c->stream, c->sm_count);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), cursor, nv * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
-        cudaFree(cursor);
+        dev_free(c, cursor);
         return set_error(DPG_ERR_CUDA, std::string("transpose counts: ") + cudaGetErrorString(e));
     }
     int64_t acc = 0;
@@ -400,16 +416,16 @@ dpg_status ensure_transpose(dpg_graph* g) {
         acc += cnt;
     }
     h[nv] = static_cast<int32_t>(acc);
-    e = cudaMalloc(&g->t_off, (nv + 1) * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&g->t_col, static_cast<size_t>(g->E > 0 ? g->E : 1) * 4);
+    e = dev_alloc(c, &g->t_off, (nv + 1) * 4);
+    if (e == cudaSuccess) e = dev_alloc(c, &g->t_col, static_cast<size_t>(g->E > 0 ? g->E : 1) * 4);
     if (e == cudaSuccess) e = cudaMemcpyAsync(g->t_off, h.data(), (nv + 1) * 4, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(cursor, h.data(), nv * 4, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = launch_transpose_scatter(g->off, g->col, g->V, cursor, g->t_col, c->stream, c->sm_count);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    cudaFree(cursor);
+    dev_free(c, cursor);
     if (e != cudaSuccess) {
-        cudaFree(g->t_off);
-        cudaFree(g->t_col);
+        dev_free(c, g->t_off);
+        dev_free(c, g->t_col);
         g->t_off = g->t_col = nullptr;
         return set_error(DPG_ERR_CUDA, std::string("transpose build: ") + cudaGetErrorString(e));
     }
@@ -688,9 +704,9 @@ dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* 
     dpg_status s = validate_offsets(g->h_off.data(), V, E, &g->max_degree);
     if (s != DPG_OK) return fail(s);
     const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    if ((e = cudaMalloc(&g->off, sizeof(int32_t) * (static_cast<size_t>(V) + 1))) != cudaSuccess ||
-        (e = cudaMalloc(&g->col, sizeof(int32_t) * static_cast<size_t>(E > 0 ? E : 1))) != cudaSuccess ||
-        (g->weighted && (e = cudaMalloc(&g->adj, sizeof(int2) * static_cast<size_t>(E > 0 ? E : 1))) != cudaSuccess))
+    if ((e = dev_alloc(c, &g->off, sizeof(int32_t) * (static_cast<size_t>(V) + 1))) != cudaSuccess ||
+        (e = dev_alloc(c, &g->col, sizeof(int32_t) * static_cast<size_t>(E > 0 ? E : 1))) != cudaSuccess ||
+        (g->weighted && (e = dev_alloc(c, &g->adj, sizeof(int2) * static_cast<size_t>(E > 0 ? E : 1))) != cudaSuccess))
         return fail(set_error(DPG_ERR_CAPACITY, std::string("graph allocation: ") + cudaGetErrorString(e)));
     if ((e = cudaMemcpyAsync(g->off, offsets, sizeof(int32_t) * (static_cast<size_t>(V) + 1), kind, c->stream)) != cudaSuccess ||
         (E > 0 && (e = cudaMemcpyAsync(g->col, col, sizeof(int32_t) * static_cast<size_t>(E), kind, c->stream)) != cudaSuccess))
@@ -869,6 +885,21 @@ dpg_status dpg_ctx_create(int device, dpg_ctx** out) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (e == cudaSuccess) e = cudaMalloc(&c->st, sizeof(DevStatus));
     if (e == cudaSuccess) e = cudaMemset(c->st, 0, sizeof(DevStatus));
+    int pools = 0;
+    if (e == cudaSuccess && cudaDeviceGetAttribute(&pools, cudaDevAttrMemoryPoolsSupported, device) == cudaSuccess && pools) {
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        if (cudaMemPoolCreate(&c->pool, &props) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool for the next graph
+            cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        } else {
+            c->pool = nullptr;
+            cudaGetLastError();
+        }
+    }
     if (e != cudaSuccess) {
         if (c->own_stream) cudaStreamDestroy(c->own_stream);
         cudaFree(c->st);
@@ -889,6 +920,8 @@ dpg_status dpg_ctx_destroy(dpg_ctx* c) {
     for (auto& b : c->bufs) cudaFree(b.p);
     cudaFree(c->st);
     cudaFree(c->trace);
+    // Blocks still held by orphaned graphs keep the pool alive until they are freed.
+    if (c->pool) cudaMemPoolDestroy(c->pool);
     cudaStreamDestroy(c->own_stream);
     delete c;
     return DPG_OK;

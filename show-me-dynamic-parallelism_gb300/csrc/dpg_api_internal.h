@@ -130,6 +130,9 @@ struct dpg_ctx {
     // becomes null) so that destroying them afterwards frees their memory without touching it.
     std::unordered_set<dpg_graph*> graphs;
     std::unordered_set<dpg_batch*> batches;
+    // Stream-ordered pool for graph-owned memory (CSR, plans, renaming, transposes). It keeps freed
+    // blocks, so graphs created and destroyed per call (the one-shot entry points) reuse them.
+    cudaMemPool_t pool = nullptr;
 };
 
 struct dpg_graph {
@@ -172,6 +175,14 @@ struct dpg_graph {
 namespace dpg_api {
 
 dpg_status use_device(dpg_ctx* c);
+// Graph-owned device memory: from the context's pool on its stream; freed stream-ordered, or
+// synchronously when the context is gone (orphaned graphs).
+cudaError_t dev_alloc(dpg_ctx* c, void** p, size_t bytes);
+template <class T>
+cudaError_t dev_alloc(dpg_ctx* c, T** p, size_t bytes) {
+    return dev_alloc(c, reinterpret_cast<void**>(p), bytes);
+}
+void dev_free(dpg_ctx* c, void* p);
 void* arena(dpg_ctx* c, Slot s, size_t bytes, dpg_status* status);
 dpg_status check_device(dpg_ctx* c);
 dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
