@@ -206,7 +206,12 @@ void graph_free_device(dpg_graph* g) {
 dpg_status ensure_plan(dpg_graph* g) {
     if (g->plan_ready) return DPG_OK;
     RowPlanHost hp;
-    build_row_plan(g->h_off.data(), g->V, &hp);
+    if (g->h_plan) {
+        hp = std::move(*g->h_plan);
+        g->h_plan.reset();
+    } else {
+        build_row_plan(g->h_off.data(), g->V, &hp);
+    }
     RowPlanDev d;
     d.ntiles = static_cast<int32_t>(hp.tiles.size());
     d.nhub_small = static_cast<int32_t>(hp.hubs_small.size());
@@ -676,7 +681,7 @@ dpg_status run_spmv(dpg_ctx* c, dpg_graph* g, const float* d_vals, const float* 
 }
 
 dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
-                               const int32_t* weights, bool device_ptrs, dpg_graph** out) {
+                               const int32_t* weights, bool device_ptrs, dpg_graph** out, bool early_plan) {
     if (!out) return set_error(DPG_ERR_INVALID_ARG, "null output handle");
     *out = nullptr;
     DPG_TRY(use_device(c));
@@ -699,7 +704,10 @@ dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* 
         e = cudaMemcpy(g->h_off.data(), offsets, sizeof(int32_t) * (static_cast<size_t>(V) + 1), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return fail(set_error(DPG_ERR_CUDA, std::string("offsets D2H: ") + cudaGetErrorString(e)));
     } else {
-        memcpy(g->h_off.data(), offsets, sizeof(int32_t) * (static_cast<size_t>(V) + 1));
+        const int64_t n = static_cast<int64_t>(V) + 1;
+        int32_t* dst = g->h_off.data();
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) dst[i] = offsets[i];
     }
     dpg_status s = validate_offsets(g->h_off.data(), V, E, &g->max_degree);
     if (s != DPG_OK) return fail(s);
@@ -724,6 +732,11 @@ dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* 
                 return fail(set_error(DPG_ERR_CUDA, std::string("weights copy: ") + cudaGetErrorString(e)));
             d_w = tmp;
         }
+    }
+    // The row plan needs only the (validated) offsets: built here, it overlaps the upload above.
+    if (early_plan) {
+        g->h_plan.reset(new RowPlanHost());
+        build_row_plan(g->h_off.data(), g->V, g->h_plan.get());
     }
     s = graph_finish(c, g, d_w);
     if (s != DPG_OK) return fail(s);
@@ -1279,7 +1292,8 @@ dpg_status dpg_sssp_host(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offset
 dpg_status dpg_pagerank_f32_host(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in_offsets, const int32_t* in_col,
                                  const int32_t* outdeg, const dpg_pr_opts* opts, float* h_rank) {
     dpg_graph* g = nullptr;
-    DPG_TRY(dpg_graph_create(c, V, E, in_offsets, in_col, nullptr, &g));
+    DPG_TRY(use_device(c));
+    DPG_TRY(graph_create_common(c, V, E, in_offsets, in_col, nullptr, false, &g, /*early_plan=*/true));
     const dpg_status s = dpg_pagerank_f32(c, g, outdeg, opts, h_rank);
     dpg_graph_destroy(g);
     return s;

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <string>
 #include <unordered_set>
 #include <vector>
@@ -149,6 +150,7 @@ struct dpg_graph {
     double mean_weight = 0.0;  // weighted graphs: mean arc weight (the near-far step default)
     bool plan_ready = false;
     RowPlanDev plan;
+    std::unique_ptr<RowPlanHost> h_plan;  // built at creation by the one-shot entry points
     // Column renaming by frequency for the row gathers (dpg_layout.cu); built on first use.
     bool relabel = true;
     bool relabel_ready = false;
@@ -186,7 +188,7 @@ void dev_free(dpg_ctx* c, void* p);
 void* arena(dpg_ctx* c, Slot s, size_t bytes, dpg_status* status);
 dpg_status check_device(dpg_ctx* c);
 dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
-                               const int32_t* weights, bool device_ptrs, dpg_graph** out);
+                               const int32_t* weights, bool device_ptrs, dpg_graph** out, bool early_plan = false);
 dpg_status ensure_plan(dpg_graph* g);
 dpg_status ensure_relabel(dpg_graph* g);
 int32_t hot_entries(const dpg_ctx* c, const dpg_graph* g);
