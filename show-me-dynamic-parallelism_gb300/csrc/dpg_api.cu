@@ -681,7 +681,7 @@ dpg_status run_spmv(dpg_ctx* c, dpg_graph* g, const float* d_vals, const float* 
 }
 
 dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
-                               const int32_t* weights, bool device_ptrs, dpg_graph** out, bool early_plan) {
+                               const int32_t* weights, bool device_ptrs, dpg_graph** out) {
     if (!out) return set_error(DPG_ERR_INVALID_ARG, "null output handle");
     *out = nullptr;
     DPG_TRY(use_device(c));
@@ -733,13 +733,112 @@ dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* 
             d_w = tmp;
         }
     }
-    // The row plan needs only the (validated) offsets: built here, it overlaps the upload above.
-    if (early_plan) {
-        g->h_plan.reset(new RowPlanHost());
-        build_row_plan(g->h_off.data(), g->V, g->h_plan.get());
-    }
     s = graph_finish(c, g, d_w);
     if (s != DPG_OK) return fail(s);
+    c->graphs.insert(g);
+    *out = g;
+    return DPG_OK;
+}
+
+// The pull graph of a one-shot PageRank (unweighted in-edge CSR from host arrays, V > 0, E > 0),
+// with the column renaming overlapped with the upload instead of run after it:
+//   - in an in-edge CSR a vertex's column count is its out-degree, so the frequency order is built
+//     from the out-degrees (copied ahead of the columns) on the aux stream while the columns upload.
+//     The order is only a renaming and every row keeps its nonzero order, so sums are identical
+//     with any order; out-degrees that disagree with the columns only make the hot cache colder;
+//   - the columns upload in kRelabelChunks pieces, and each piece is range-checked and renamed on
+//     the aux stream as soon as it has landed. That check replaces graph_finish's separate pass:
+//     an out-of-range column fails the creation exactly as graph_finish would.
+// d_outdeg (V ints) receives the out-degrees for the sweeps. The row plan is built on the host
+// meanwhile.
+dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in_offsets, const int32_t* in_col,
+                             const int32_t* h_outdeg, int32_t* d_outdeg, dpg_graph** out) {
+    constexpr int kRelabelChunks = 8;
+    *out = nullptr;
+    dpg_graph* g = new dpg_graph();
+    g->ctx = c;
+    g->device = c->device;
+    g->V = V;
+    g->E = E;
+    const size_t nv = static_cast<size_t>(V), ne = static_cast<size_t>(E);
+    g->h_off.resize(nv + 1);
+    {
+        const int64_t n = static_cast<int64_t>(nv) + 1;
+        int32_t* dst = g->h_off.data();
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) dst[i] = in_offsets[i];
+    }
+    int32_t* scratch = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_done = nullptr, ev_chunk[kRelabelChunks] = {};
+    auto release = [&]() {
+        if (c->aux_stream) cudaStreamSynchronize(c->aux_stream);
+        dev_free(c, scratch);
+        scratch = nullptr;
+        for (cudaEvent_t ev : ev_chunk)
+            if (ev) cudaEventDestroy(ev);
+        if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_done) cudaEventDestroy(ev_done);
+        ev_in = ev_done = nullptr;
+        for (cudaEvent_t& ev : ev_chunk) ev = nullptr;
+    };
+    auto fail = [&](dpg_status s) {
+        release();
+        graph_free_device(g);
+        delete g;
+        return s;
+    };
+    dpg_status s = validate_offsets(g->h_off.data(), V, E, &g->max_degree);
+    if (s != DPG_OK) return fail(s);
+    cudaError_t e = cudaSuccess;
+    if (!c->aux_stream && (e = cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        c->aux_stream = nullptr;
+        return fail(set_error(DPG_ERR_CUDA, std::string("aux stream: ") + cudaGetErrorString(e)));
+    }
+    dpg_status as = DPG_OK;
+    int* bad = static_cast<int*>(arena(c, S_NONSTOP, sizeof(int) * 4, &as));
+    if (!bad) return fail(as);
+    if ((e = dev_alloc(c, &g->off, (nv + 1) * 4)) != cudaSuccess || (e = dev_alloc(c, &g->col, ne * 4)) != cudaSuccess ||
+        (e = dev_alloc(c, &g->perm, nv * 4)) != cudaSuccess || (e = dev_alloc(c, &g->inv, nv * 4)) != cudaSuccess ||
+        (e = dev_alloc(c, &g->pcol, ne * 4)) != cudaSuccess ||
+        (e = dev_alloc(c, &scratch, frequency_order_scratch_bytes(V))) != cudaSuccess)
+        return fail(set_error(DPG_ERR_CAPACITY, std::string("graph allocation: ") + cudaGetErrorString(e)));
+    if ((e = cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming)) != cudaSuccess)
+        return fail(set_error(DPG_ERR_CUDA, std::string("events: ") + cudaGetErrorString(e)));
+    for (cudaEvent_t& ev : ev_chunk)
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+            return fail(set_error(DPG_ERR_CUDA, std::string("events: ") + cudaGetErrorString(e)));
+    cudaStream_t s0 = c->stream, s1 = c->aux_stream;
+    // Upload stream: flag reset, offsets, out-degrees, then the column chunks, each with an event.
+    if ((e = cudaMemsetAsync(bad, 0, sizeof(int), s0)) == cudaSuccess &&
+        (e = cudaMemcpyAsync(g->off, in_offsets, (nv + 1) * 4, cudaMemcpyHostToDevice, s0)) == cudaSuccess &&
+        (e = cudaMemcpyAsync(d_outdeg, h_outdeg, nv * 4, cudaMemcpyHostToDevice, s0)) == cudaSuccess)
+        e = cudaEventRecord(ev_in, s0);
+    const int64_t step = (E + kRelabelChunks - 1) / kRelabelChunks;
+    for (int k = 0; k < kRelabelChunks && e == cudaSuccess; ++k) {
+        const int64_t b = std::min<int64_t>(E, k * step), n = std::min<int64_t>(E, b + step) - b;
+        if (n > 0) e = cudaMemcpyAsync(g->col + b, in_col + b, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, s0);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_chunk[k], s0);
+    }
+    // Aux stream: the order once the out-degrees are in, then each chunk once it has landed.
+    if (e == cudaSuccess && (e = cudaStreamWaitEvent(s1, ev_in, 0)) == cudaSuccess)
+        e = launch_frequency_order(d_outdeg, V, scratch, g->perm, g->inv, s1);
+    for (int k = 0; k < kRelabelChunks && e == cudaSuccess; ++k) {
+        const int64_t b = std::min<int64_t>(E, k * step), n = std::min<int64_t>(E, b + step) - b;
+        if ((e = cudaStreamWaitEvent(s1, ev_chunk[k], 0)) == cudaSuccess)
+            e = launch_relabel_columns(g->col + b, g->perm, n, g->pcol + b, s1, c->sm_count, V, bad);
+    }
+    if (e == cudaSuccess && (e = cudaEventRecord(ev_done, s1)) == cudaSuccess) e = cudaStreamWaitEvent(s0, ev_done, 0);
+    if (e != cudaSuccess) return fail(set_error(DPG_ERR_CUDA, std::string("graph upload: ") + cudaGetErrorString(e)));
+    g->h_plan.reset(new RowPlanHost());
+    build_row_plan(g->h_off.data(), V, g->h_plan.get());
+    int hbad = 0;
+    if ((e = cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s0)) == cudaSuccess)
+        e = cudaStreamSynchronize(s0);
+    if (e != cudaSuccess) return fail(set_error(DPG_ERR_CUDA, std::string("graph upload: ") + cudaGetErrorString(e)));
+    if (hbad & 1) return fail(set_error(DPG_ERR_INVALID_ARG, "column index out of range"));
+    release();
+    g->relabel_ready = true;
     c->graphs.insert(g);
     *out = g;
     return DPG_OK;
@@ -935,6 +1034,10 @@ dpg_status dpg_ctx_destroy(dpg_ctx* c) {
     cudaFree(c->trace);
     // Blocks still held by orphaned graphs keep the pool alive until they are freed.
     if (c->pool) cudaMemPoolDestroy(c->pool);
+    if (c->aux_stream) {
+        cudaStreamSynchronize(c->aux_stream);
+        cudaStreamDestroy(c->aux_stream);
+    }
     cudaStreamDestroy(c->own_stream);
     delete c;
     return DPG_OK;
@@ -1293,8 +1396,24 @@ dpg_status dpg_pagerank_f32_host(dpg_ctx* c, int32_t V, int64_t E, const int32_t
                                  const int32_t* outdeg, const dpg_pr_opts* opts, float* h_rank) {
     dpg_graph* g = nullptr;
     DPG_TRY(use_device(c));
-    DPG_TRY(graph_create_common(c, V, E, in_offsets, in_col, nullptr, false, &g, /*early_plan=*/true));
-    const dpg_status s = dpg_pagerank_f32(c, g, outdeg, opts, h_rank);
+    if (V <= 0 || E <= 0 || E > INT32_MAX || !in_offsets || !in_col || !outdeg || !h_rank) {
+        // Empty graphs and argument errors: the general path, which reports them.
+        DPG_TRY(graph_create_common(c, V, E, in_offsets, in_col, nullptr, false, &g));
+        const dpg_status s = dpg_pagerank_f32(c, g, outdeg, opts, h_rank);
+        dpg_graph_destroy(g);
+        return s;
+    }
+    dpg_status st = DPG_OK;
+    const size_t nv = static_cast<size_t>(V);
+    int32_t* dod = static_cast<int32_t*>(arena(c, S_OUTDEG, nv * 4, &st));
+    float* dr = static_cast<float*>(arena(c, S_RANKOUT, nv * 4, &st));
+    if (st != DPG_OK) return st;
+    DPG_TRY(graph_create_pull(c, V, E, in_offsets, in_col, outdeg, dod, &g));
+    dpg_status s = run_pagerank(c, g, dod, opts, dr);
+    if (s == DPG_OK) {
+        const cudaError_t e = cudaMemcpyAsync(h_rank, dr, nv * 4, cudaMemcpyDeviceToHost, c->stream);
+        s = e == cudaSuccess ? check_device(c) : set_error(DPG_ERR_CUDA, cudaGetErrorString(e));
+    }
     dpg_graph_destroy(g);
     return s;
 }

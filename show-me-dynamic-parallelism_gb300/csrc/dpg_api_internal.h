@@ -134,6 +134,8 @@ struct dpg_ctx {
     // Stream-ordered pool for graph-owned memory (CSR, plans, renaming, transposes). It keeps freed
     // blocks, so graphs created and destroyed per call (the one-shot entry points) reuse them.
     cudaMemPool_t pool = nullptr;
+    // Second stream, created on first use: work that overlaps an upload on `stream` (event-ordered).
+    cudaStream_t aux_stream = nullptr;
 };
 
 struct dpg_graph {
@@ -188,7 +190,9 @@ void dev_free(dpg_ctx* c, void* p);
 void* arena(dpg_ctx* c, Slot s, size_t bytes, dpg_status* status);
 dpg_status check_device(dpg_ctx* c);
 dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
-                               const int32_t* weights, bool device_ptrs, dpg_graph** out, bool early_plan = false);
+                               const int32_t* weights, bool device_ptrs, dpg_graph** out);
+dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in_offsets, const int32_t* in_col,
+                             const int32_t* h_outdeg, int32_t* d_outdeg, dpg_graph** out);
 dpg_status ensure_plan(dpg_graph* g);
 dpg_status ensure_relabel(dpg_graph* g);
 int32_t hot_entries(const dpg_ctx* c, const dpg_graph* g);

@@ -261,8 +261,10 @@ cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s, int sm
 
 // Column renaming by frequency (dpg_layout.cu).
 cudaError_t launch_column_histogram(const int32_t* col, int64_t E, int32_t* counts, cudaStream_t s, int sm_count);
+// out[e] = perm[col[e]] for e < E. With `bad`, columns are range-checked against V on the way
+// (an out-of-range one sets *bad |= 1 and writes 0) for uploads whose columns were not yet checked.
 cudaError_t launch_relabel_columns(const int32_t* col, const int32_t* perm, int64_t E, int32_t* out, cudaStream_t s,
-                                   int sm_count);
+                                   int sm_count, int32_t V = 0, int* bad = nullptr);
 cudaError_t launch_gather_by_index(const float* x, const int32_t* inv, int32_t V, float* out, cudaStream_t s,
                                    int sm_count);
 // Transposed CSR on the device: t_col[t_off[v] .. t_off[v+1]) lists the u with v in row u (order

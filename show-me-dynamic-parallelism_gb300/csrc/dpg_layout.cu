@@ -35,6 +35,20 @@ __global__ void relabel_columns_kernel(const int32_t* __restrict__ col, const in
         out[e] = __ldg(perm + __ldg(col + e));
 }
 
+// The same with the range check of an unchecked upload folded in.
+__global__ void relabel_check_columns_kernel(const int32_t* __restrict__ col, const int32_t* __restrict__ perm,
+                                             int64_t E, int32_t V, int32_t* __restrict__ out, int* bad) {
+    bool any = false;
+    for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < E;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int32_t c = __ldg(col + e);
+        const bool ok = static_cast<uint32_t>(c) < static_cast<uint32_t>(V);
+        any |= !ok;
+        out[e] = ok ? __ldg(perm + c) : 0;
+    }
+    if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(bad, 1);
+}
+
 __global__ void gather_by_index_kernel(const float* __restrict__ x, const int32_t* __restrict__ inv, int32_t V,
                                        float* __restrict__ out) {
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < V;
@@ -172,8 +186,10 @@ cudaError_t launch_column_histogram(const int32_t* col, int64_t E, int32_t* coun
 }
 
 cudaError_t launch_relabel_columns(const int32_t* col, const int32_t* perm, int64_t E, int32_t* out, cudaStream_t s,
-                                   int sm_count) {
-    if (E > 0) relabel_columns_kernel<<<sm_count * 8, 256, 0, s>>>(col, perm, E, out);
+                                   int sm_count, int32_t V, int* bad) {
+    if (E <= 0) return cudaGetLastError();
+    if (bad) relabel_check_columns_kernel<<<sm_count * 8, 256, 0, s>>>(col, perm, E, V, out, bad);
+    else relabel_columns_kernel<<<sm_count * 8, 256, 0, s>>>(col, perm, E, out);
     return cudaGetLastError();
 }
 

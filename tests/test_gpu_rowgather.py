@@ -159,6 +159,37 @@ def test_one_shot_pagerank_host_call(ctx, orc, graphs):
     assert np.max(np.abs(r - r64) / r64) <= TOL
 
 
+@pytest.mark.parametrize("name", ["rmat12", "hubs", "data_test"])
+def test_one_shot_matches_graph_path_bitwise(ctx, graphs, name):
+    # The one-shot call renames columns by the out-degree array while the columns upload; the graph
+    # path renames them by a column histogram. Rows keep their nonzero order either way, so the
+    # ranks are the same bits, also when the out-degrees disagree with the columns (the order then
+    # differs from the histogram's).
+    g = graphs[name]
+    in_off, in_col, od = _pr_inputs(g)
+    rng = np.random.default_rng(17)
+    for outdeg in (od, rng.permutation(od).astype(np.int32)):
+        one = dpg.pagerank_host(ctx, in_off, in_col, outdeg, iterations=20)
+        two = dpg.pagerank(ctx, dpg.Graph(ctx, in_off, in_col), outdeg, iterations=20)
+        assert np.array_equal(one.view(np.uint32), two.view(np.uint32))
+
+
+def test_one_shot_rejects_bad_columns(ctx, graphs):
+    g = graphs["rmat12"]
+    in_off, in_col, od = _pr_inputs(g)
+    for bad in (g.V, -1, 1 << 30):
+        col = in_col.copy()
+        col[len(col) // 2 + 3] = bad
+        with pytest.raises(dpg.DpgError) as e:
+            dpg.pagerank_host(ctx, in_off, col, od)
+        assert e.value.status == dpg.ERR_INVALID_ARG
+        assert "column index out of range" in str(e.value)
+    # The context stays usable, and the next one-shot call is right.
+    r = dpg.pagerank_host(ctx, in_off, in_col, od, iterations=20)
+    ref = dpg.pagerank(ctx, dpg.Graph(ctx, in_off, in_col), od, iterations=20)
+    assert np.array_equal(r.view(np.uint32), ref.view(np.uint32))
+
+
 def test_spmv_pagerank_rmat22_full_size(ctx, orc):
     # R-MAT scale 22, edge factor 16; FP32 values uniform in (0,1], x uniform in [-1,1];
     # PageRank d = 0.85, 20 iterations, dangling mass spread uniformly.
@@ -171,6 +202,8 @@ def test_spmv_pagerank_rmat22_full_size(ctx, orc):
     r = dpg.pagerank(ctx, dpg.Graph(ctx, in_off, in_col), od, iterations=20)
     r64, _ = orc.pagerank_f64(in_off, in_col, od, iterations=20)
     assert np.max(np.abs(r - r64) / r64) <= TOL
+    one = dpg.pagerank_host(ctx, in_off, in_col, od, iterations=20)
+    assert np.array_equal(one.view(np.uint32), r.view(np.uint32))
 
 
 @pytest.mark.parametrize("name", ["rmat16", "hubs"])
