@@ -203,39 +203,86 @@ void graph_free_device(dpg_graph* g) {
     g->plan = RowPlanDev();
 }
 
-dpg_status ensure_plan(dpg_graph* g) {
-    if (g->plan_ready) return DPG_OK;
-    RowPlanHost hp;
-    if (g->h_plan) {
-        hp = std::move(*g->h_plan);
-        g->h_plan.reset();
-    } else {
-        build_row_plan(g->h_off.data(), g->V, &hp);
-    }
-    RowPlanDev d;
-    d.ntiles = static_cast<int32_t>(hp.tiles.size());
-    d.nhub_small = static_cast<int32_t>(hp.hubs_small.size());
-    d.nhub_big = static_cast<int32_t>(hp.hubs_big.size());
-    d.nseg = hp.nseg;
-    cudaStream_t s = g->ctx->stream;
+cudaError_t plan_build_alloc(dpg_ctx* c, int32_t V, int64_t E, PlanBuild* pb) {
+    pb->caps = row_plan_caps(V, E);
+    cudaError_t e;
+    if ((e = dev_alloc(c, &pb->tiles, sizeof(int4) * static_cast<size_t>(pb->caps.tiles))) != cudaSuccess ||
+        (e = dev_alloc(c, &pb->hubs_small, sizeof(int4) * static_cast<size_t>(pb->caps.hubs))) != cudaSuccess ||
+        (e = dev_alloc(c, &pb->hubs_big, sizeof(int4) * static_cast<size_t>(pb->caps.hubs))) != cudaSuccess)
+        return e;
+    return dev_alloc(c, &pb->scratch, pb->caps.scratch_bytes);
+}
+
+cudaError_t plan_build_launch(const PlanBuild& pb, const int32_t* d_off, int32_t V, int64_t E, PlanInfo* d_info,
+                              cudaStream_t s) {
+    return launch_build_row_plan(d_off, V, E, pb.caps, pb.tiles, pb.hubs_small, pb.hubs_big, pb.scratch,
+                                 d_info->totals, &d_info->bad, s);
+}
+
+void plan_build_free(dpg_ctx* c, PlanBuild* pb) {
+    dev_free(c, pb->tiles);
+    dev_free(c, pb->hubs_small);
+    dev_free(c, pb->hubs_big);
+    dev_free(c, pb->scratch);
+    *pb = PlanBuild();
+}
+
+dpg_status plan_finish(dpg_graph* g, PlanBuild* pb, const PlanInfo& info) {
     dpg_ctx* c = g->ctx;
-    DPG_CUDA_TRY(dev_alloc(c, &d.tiles, sizeof(int4) * (hp.tiles.size() + 1)));
-    DPG_CUDA_TRY(dev_alloc(c, &d.lane_r0, 32 * (hp.tiles.size() + 1)));
-    DPG_CUDA_TRY(dev_alloc(c, &d.hubs_small, sizeof(int4) * (hp.hubs_small.size() + 1)));
-    DPG_CUDA_TRY(dev_alloc(c, &d.hubs_big, sizeof(int4) * (hp.hubs_big.size() + 1)));
-    if (!hp.tiles.empty())
-        DPG_CUDA_TRY(cudaMemcpyAsync(d.tiles, hp.tiles.data(), sizeof(int4) * hp.tiles.size(), cudaMemcpyHostToDevice, s));
-    if (!hp.hubs_small.empty())
-        DPG_CUDA_TRY(cudaMemcpyAsync(d.hubs_small, hp.hubs_small.data(), sizeof(int4) * hp.hubs_small.size(),
-                                     cudaMemcpyHostToDevice, s));
-    if (!hp.hubs_big.empty())
-        DPG_CUDA_TRY(cudaMemcpyAsync(d.hubs_big, hp.hubs_big.data(), sizeof(int4) * hp.hubs_big.size(),
-                                     cudaMemcpyHostToDevice, s));
-    DPG_CUDA_TRY(launch_tile_lane_starts(d, g->off, s, g->ctx->sm_count));
-    DPG_CUDA_TRY(cudaStreamSynchronize(s));
+    cudaStream_t s = c->stream;
+    const int64_t nt = info.totals[0], nsm = info.totals[1], nbg = info.totals[2], nsg = info.totals[3];
+    if (nt < 0 || nt > pb->caps.tiles || nsm < 0 || nsm > pb->caps.hubs || nbg < 0 || nbg > pb->caps.hubs || nsg < 0 ||
+        nsg > INT32_MAX)
+        return set_error(DPG_ERR_CAPACITY, "row plan exceeds its capacity");
+    RowPlanDev d;
+    d.ntiles = static_cast<int32_t>(nt);
+    d.nhub_small = static_cast<int32_t>(nsm);
+    d.nhub_big = static_cast<int32_t>(nbg);
+    d.nseg = static_cast<int32_t>(nsg);
+    DPG_CUDA_TRY(dev_alloc(c, &d.tiles, sizeof(int4) * static_cast<size_t>(nt + 1)));
+    DPG_CUDA_TRY(dev_alloc(c, &d.lane_r0, 32 * static_cast<size_t>(nt + 1)));
+    DPG_CUDA_TRY(dev_alloc(c, &d.hubs_small, sizeof(int4) * static_cast<size_t>(nsm + 1)));
+    DPG_CUDA_TRY(dev_alloc(c, &d.hubs_big, sizeof(int4) * static_cast<size_t>(nbg + 1)));
+    if (nt > 0)
+        DPG_CUDA_TRY(cudaMemcpyAsync(d.tiles, pb->tiles, sizeof(int4) * static_cast<size_t>(nt), cudaMemcpyDeviceToDevice, s));
+    if (nsm > 0)
+        DPG_CUDA_TRY(cudaMemcpyAsync(d.hubs_small, pb->hubs_small, sizeof(int4) * static_cast<size_t>(nsm),
+                                     cudaMemcpyDeviceToDevice, s));
+    if (nbg > 0)
+        DPG_CUDA_TRY(cudaMemcpyAsync(d.hubs_big, pb->hubs_big, sizeof(int4) * static_cast<size_t>(nbg),
+                                     cudaMemcpyDeviceToDevice, s));
+    plan_build_free(c, pb);
+    DPG_CUDA_TRY(launch_tile_lane_starts(d, g->off, s, c->sm_count));
     g->plan = d;
     g->plan_ready = true;
     return DPG_OK;
+}
+
+// The row plan of a graph whose offsets were validated on the host at creation.
+dpg_status ensure_plan(dpg_graph* g) {
+    if (g->plan_ready) return DPG_OK;
+    dpg_ctx* c = g->ctx;
+    dpg_status st = DPG_OK;
+    PlanInfo* info = static_cast<PlanInfo*>(arena(c, S_PLANINFO, sizeof(PlanInfo), &st));
+    if (!info) return st;
+    PlanBuild pb;
+    cudaError_t e = cudaMemsetAsync(info, 0, sizeof(PlanInfo), c->stream);
+    if (e == cudaSuccess) e = plan_build_alloc(c, g->V, g->E, &pb);
+    if (e == cudaSuccess) e = plan_build_launch(pb, g->off, g->V, g->E, info, c->stream);
+    PlanInfo h;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, info, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        plan_build_free(c, &pb);
+        return set_error(DPG_ERR_CUDA, std::string("row plan: ") + cudaGetErrorString(e));
+    }
+    if (h.bad & 4) {
+        plan_build_free(c, &pb);
+        return set_error(DPG_ERR_INVALID_ARG, "offsets are not a valid CSR");
+    }
+    const dpg_status fs = plan_finish(g, &pb, h);
+    if (fs != DPG_OK) plan_build_free(c, &pb);
+    return fs;
 }
 
 // Entries of the gathered vector kept in shared memory by the row-gather kernel: as many of the
@@ -740,17 +787,20 @@ dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* 
     return DPG_OK;
 }
 
-// The pull graph of a one-shot PageRank (unweighted in-edge CSR from host arrays, V > 0, E > 0),
-// with the column renaming overlapped with the upload instead of run after it:
-//   - in an in-edge CSR a vertex's column count is its out-degree, so the frequency order is built
-//     from the out-degrees (copied ahead of the columns) on the aux stream while the columns upload.
-//     The order is only a renaming and every row keeps its nonzero order, so sums are identical
-//     with any order; out-degrees that disagree with the columns only make the hot cache colder;
-//   - the columns upload in kRelabelChunks pieces, and each piece is range-checked and renamed on
-//     the aux stream as soon as it has landed. That check replaces graph_finish's separate pass:
-//     an out-of-range column fails the creation exactly as graph_finish would.
-// d_outdeg (V ints) receives the out-degrees for the sweeps. The row plan is built on the host
-// meanwhile.
+// The pull graph of a one-shot PageRank (unweighted in-edge CSR from host arrays, V > 0, E > 0).
+// Everything between the upload and the sweeps runs on the device, on the aux stream, overlapped
+// with the upload of the columns; the host only issues work and waits once:
+//   - the offsets and out-degrees upload first. Then the offsets are validated on the device and
+//     the row plan is built on the device from them;
+//   - in an in-edge CSR a vertex's column count is its out-degree, so the frequency order of the
+//     column renaming comes from the out-degrees. The order is only a renaming and every row keeps
+//     its nonzero order, so the sums are the same with any order; out-degrees that disagree with
+//     the columns only make the hot cache colder;
+//   - the columns upload in kRelabelChunks pieces, and each piece is range-checked and renamed as
+//     soon as it has landed (the check graph_finish would make).
+// Bad offsets or columns fail the creation with graph_create_common's errors. The graph keeps no
+// host copy of its offsets (h_off is empty): it serves the PageRank sweeps only.
+// d_outdeg (V ints) receives the out-degrees for the sweeps.
 dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in_offsets, const int32_t* in_col,
                              const int32_t* h_outdeg, int32_t* d_outdeg, dpg_graph** out) {
     constexpr int kRelabelChunks = 8;
@@ -761,25 +811,21 @@ dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in
     g->V = V;
     g->E = E;
     const size_t nv = static_cast<size_t>(V), ne = static_cast<size_t>(E);
-    g->h_off.resize(nv + 1);
-    {
-        const int64_t n = static_cast<int64_t>(nv) + 1;
-        int32_t* dst = g->h_off.data();
-#pragma omp parallel for schedule(static)
-        for (int64_t i = 0; i < n; ++i) dst[i] = in_offsets[i];
-    }
     int32_t* scratch = nullptr;
+    PlanBuild pb;
     cudaEvent_t ev_in = nullptr, ev_done = nullptr, ev_chunk[kRelabelChunks] = {};
     auto release = [&]() {
         if (c->aux_stream) cudaStreamSynchronize(c->aux_stream);
         dev_free(c, scratch);
         scratch = nullptr;
-        for (cudaEvent_t ev : ev_chunk)
+        plan_build_free(c, &pb);
+        for (cudaEvent_t& ev : ev_chunk) {
             if (ev) cudaEventDestroy(ev);
+            ev = nullptr;
+        }
         if (ev_in) cudaEventDestroy(ev_in);
         if (ev_done) cudaEventDestroy(ev_done);
         ev_in = ev_done = nullptr;
-        for (cudaEvent_t& ev : ev_chunk) ev = nullptr;
     };
     auto fail = [&](dpg_status s) {
         release();
@@ -787,20 +833,20 @@ dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in
         delete g;
         return s;
     };
-    dpg_status s = validate_offsets(g->h_off.data(), V, E, &g->max_degree);
-    if (s != DPG_OK) return fail(s);
     cudaError_t e = cudaSuccess;
     if (!c->aux_stream && (e = cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking)) != cudaSuccess) {
         c->aux_stream = nullptr;
         return fail(set_error(DPG_ERR_CUDA, std::string("aux stream: ") + cudaGetErrorString(e)));
     }
     dpg_status as = DPG_OK;
-    int* bad = static_cast<int*>(arena(c, S_NONSTOP, sizeof(int) * 4, &as));
-    if (!bad) return fail(as);
+    PlanInfo* info = static_cast<PlanInfo*>(arena(c, S_PLANINFO, sizeof(PlanInfo), &as));
+    if (!info) return fail(as);
+    cudaStream_t s0 = c->stream, s1 = c->aux_stream;
     if ((e = dev_alloc(c, &g->off, (nv + 1) * 4)) != cudaSuccess || (e = dev_alloc(c, &g->col, ne * 4)) != cudaSuccess ||
         (e = dev_alloc(c, &g->perm, nv * 4)) != cudaSuccess || (e = dev_alloc(c, &g->inv, nv * 4)) != cudaSuccess ||
         (e = dev_alloc(c, &g->pcol, ne * 4)) != cudaSuccess ||
-        (e = dev_alloc(c, &scratch, frequency_order_scratch_bytes(V))) != cudaSuccess)
+        (e = dev_alloc(c, &scratch, frequency_order_scratch_bytes(V))) != cudaSuccess ||
+        (e = plan_build_alloc(c, V, E, &pb)) != cudaSuccess)
         return fail(set_error(DPG_ERR_CAPACITY, std::string("graph allocation: ") + cudaGetErrorString(e)));
     if ((e = cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming)) != cudaSuccess)
@@ -808,9 +854,10 @@ dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in
     for (cudaEvent_t& ev : ev_chunk)
         if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
             return fail(set_error(DPG_ERR_CUDA, std::string("events: ") + cudaGetErrorString(e)));
-    cudaStream_t s0 = c->stream, s1 = c->aux_stream;
-    // Upload stream: flag reset, offsets, out-degrees, then the column chunks, each with an event.
-    if ((e = cudaMemsetAsync(bad, 0, sizeof(int), s0)) == cudaSuccess &&
+    // Everything the aux stream touches is allocated above, before ev_in is recorded on s0, so
+    // waiting for ev_in also orders the aux stream after those stream-ordered allocations.
+    // Upload stream: status reset, offsets, out-degrees, then the column chunks, each with an event.
+    if ((e = cudaMemsetAsync(info, 0, sizeof(PlanInfo), s0)) == cudaSuccess &&
         (e = cudaMemcpyAsync(g->off, in_offsets, (nv + 1) * 4, cudaMemcpyHostToDevice, s0)) == cudaSuccess &&
         (e = cudaMemcpyAsync(d_outdeg, h_outdeg, nv * 4, cudaMemcpyHostToDevice, s0)) == cudaSuccess)
         e = cudaEventRecord(ev_in, s0);
@@ -820,23 +867,33 @@ dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in
         if (n > 0) e = cudaMemcpyAsync(g->col + b, in_col + b, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, s0);
         if (e == cudaSuccess) e = cudaEventRecord(ev_chunk[k], s0);
     }
-    // Aux stream: the order once the out-degrees are in, then each chunk once it has landed.
-    if (e == cudaSuccess && (e = cudaStreamWaitEvent(s1, ev_in, 0)) == cudaSuccess)
-        e = launch_frequency_order(d_outdeg, V, scratch, g->perm, g->inv, s1);
+    // Aux stream, once offsets and out-degrees are in: offset check, row plan, renaming order; then
+    // each column chunk once it has landed.
+    if (e == cudaSuccess && (e = cudaStreamWaitEvent(s1, ev_in, 0)) == cudaSuccess) {
+        validate_offsets_kernel<<<c->sm_count * 4, 256, 0, s1>>>(g->off, V, E, &info->bad);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = plan_build_launch(pb, g->off, V, E, info, s1);
+    if (e == cudaSuccess) e = launch_frequency_order(d_outdeg, V, scratch, g->perm, g->inv, s1);
     for (int k = 0; k < kRelabelChunks && e == cudaSuccess; ++k) {
         const int64_t b = std::min<int64_t>(E, k * step), n = std::min<int64_t>(E, b + step) - b;
         if ((e = cudaStreamWaitEvent(s1, ev_chunk[k], 0)) == cudaSuccess)
-            e = launch_relabel_columns(g->col + b, g->perm, n, g->pcol + b, s1, c->sm_count, V, bad);
+            e = launch_relabel_columns(g->col + b, g->perm, n, g->pcol + b, s1, c->sm_count, V, &info->bad);
     }
     if (e == cudaSuccess && (e = cudaEventRecord(ev_done, s1)) == cudaSuccess) e = cudaStreamWaitEvent(s0, ev_done, 0);
-    if (e != cudaSuccess) return fail(set_error(DPG_ERR_CUDA, std::string("graph upload: ") + cudaGetErrorString(e)));
-    g->h_plan.reset(new RowPlanHost());
-    build_row_plan(g->h_off.data(), V, g->h_plan.get());
-    int hbad = 0;
-    if ((e = cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s0)) == cudaSuccess)
+    PlanInfo h;
+    if (e == cudaSuccess && (e = cudaMemcpyAsync(&h, info, sizeof(h), cudaMemcpyDeviceToHost, s0)) == cudaSuccess)
         e = cudaStreamSynchronize(s0);
     if (e != cudaSuccess) return fail(set_error(DPG_ERR_CUDA, std::string("graph upload: ") + cudaGetErrorString(e)));
-    if (hbad & 1) return fail(set_error(DPG_ERR_INVALID_ARG, "column index out of range"));
+    if (h.bad & 4) {
+        // The host check gives the precise message.
+        int32_t md = 0;
+        const dpg_status vs = validate_offsets(in_offsets, V, E, &md);
+        return fail(vs != DPG_OK ? vs : set_error(DPG_ERR_INVALID_ARG, "offsets are not a valid CSR"));
+    }
+    if (h.bad & 1) return fail(set_error(DPG_ERR_INVALID_ARG, "column index out of range"));
+    const dpg_status ps = plan_finish(g, &pb, h);
+    if (ps != DPG_OK) return fail(ps);
     release();
     g->relabel_ready = true;
     c->graphs.insert(g);

@@ -35,7 +35,7 @@ enum Slot {
     S_PRG_W, S_PRG_Y, S_PRG_C, S_PRG_V0, S_PRG_V1, S_PRG_V2, S_PRG_V3, S_PRG_PART, S_PRG_RED, S_PRG_FLAGS,
     S_DIRTY0, S_DIRTY1,
     S_CDP_BUF0, S_CDP_BUF1, S_CDP_WORDS,
-    S_TRANSPOSE, S_TRANSPOSE_ARC, S_DO_COUNT, S_FAR0, S_FAR1, S_FAR2, S_FAR_COUNT,
+    S_TRANSPOSE, S_TRANSPOSE_ARC, S_DO_COUNT, S_FAR0, S_FAR1, S_FAR2, S_FAR_COUNT, S_PLANINFO,
     S_COUNT_SLOTS
 };
 
@@ -152,7 +152,6 @@ struct dpg_graph {
     double mean_weight = 0.0;  // weighted graphs: mean arc weight (the near-far step default)
     bool plan_ready = false;
     RowPlanDev plan;
-    std::unique_ptr<RowPlanHost> h_plan;  // built at creation by the one-shot entry points
     // Column renaming by frequency for the row gathers (dpg_layout.cu); built on first use.
     bool relabel = true;
     bool relabel_ready = false;
@@ -194,6 +193,25 @@ dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* 
 dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in_offsets, const int32_t* in_col,
                              const int32_t* h_outdeg, int32_t* d_outdeg, dpg_graph** out);
 dpg_status ensure_plan(dpg_graph* g);
+// Device row-plan build: capacity buffers and the asynchronous build, then (with the totals read
+// back) exact buffers, the lane starts and the release of the build buffers.
+struct PlanInfo {
+    int64_t totals[4];  // tiles, small hubs, big hubs, segments
+    int bad;            // 1: column out of range, 4: bad offsets
+    int pad[3];
+};
+struct PlanBuild {
+    RowPlanCaps caps;
+    int4* tiles = nullptr;
+    int4* hubs_small = nullptr;
+    int4* hubs_big = nullptr;
+    void* scratch = nullptr;
+};
+cudaError_t plan_build_alloc(dpg_ctx* c, int32_t V, int64_t E, PlanBuild* pb);
+cudaError_t plan_build_launch(const PlanBuild& pb, const int32_t* d_off, int32_t V, int64_t E, PlanInfo* d_info,
+                              cudaStream_t s);
+dpg_status plan_finish(dpg_graph* g, PlanBuild* pb, const PlanInfo& info);
+void plan_build_free(dpg_ctx* c, PlanBuild* pb);
 dpg_status ensure_relabel(dpg_graph* g);
 int32_t hot_entries(const dpg_ctx* c, const dpg_graph* g);
 dpg_status pr_defaults(const dpg_pr_opts* in, dpg_pr_opts* o);

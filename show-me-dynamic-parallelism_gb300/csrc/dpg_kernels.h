@@ -124,14 +124,18 @@ constexpr int kSmallHubSegs = 8;    // hubs with at most this many segments are 
 // Tile {row, nrows, nnz_begin, nnz}: nrows > 0 covers whole rows [row, row+nrows) and exactly their
 // nonzeros; nrows < 0 is segment -(nrows+1) of hub row `row`, nonzeros [nnz_begin, nnz_begin+nnz).
 // Hub {row, first segment, segment count, 0}.
-struct RowPlanHost {
-    std::vector<int4> tiles;
-    std::vector<int4> hubs_small;
-    std::vector<int4> hubs_big;
-    int32_t nseg = 0;
+// The plan is built on the device (dpg_rowgather.cu) into buffers of the capacities below, which
+// bound any valid CSR with V rows and E nonzeros; totals[0..3] receive the tile, small-hub, big-hub
+// and segment counts, and bad offsets set *bad |= 4 (the plan is then unusable).
+struct RowPlanCaps {
+    int64_t tiles = 0;
+    int64_t hubs = 0;  // per hub list
+    size_t scratch_bytes = 0;
 };
-
-void build_row_plan(const int32_t* offsets, int32_t V, RowPlanHost* plan);
+RowPlanCaps row_plan_caps(int32_t V, int64_t E);
+cudaError_t launch_build_row_plan(const int32_t* off, int32_t V, int64_t E, const RowPlanCaps& caps, int4* tiles,
+                                  int4* hubs_small, int4* hubs_big, void* scratch, int64_t* totals, int* bad,
+                                  cudaStream_t s);
 
 struct RowPlanDev {
     int4* tiles = nullptr;

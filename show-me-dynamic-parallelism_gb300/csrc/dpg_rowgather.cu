@@ -372,64 +372,197 @@ cudaError_t prepare_rowgather(size_t bytes) {
 }  // namespace
 
 namespace {
-// Greedy tiling of rows [r0, r1): consecutive rows share a tile while their merge items (rows +
-// nonzeros) fit in kRowTileItems; rows above kHubRowDegree become hubs cut into kRowTileItems
-// segments, numbered from 0 within this range.
-void plan_rows(const int32_t* off, int32_t r0, int32_t r1, RowPlanHost* plan) {
-    int32_t cur_row = r0, cur_rows = 0, cur_items = 0;
-    auto flush = [&]() {
-        if (cur_rows > 0)
-            plan->tiles.push_back(make_int4(cur_row, cur_rows, off[cur_row], off[cur_row + cur_rows] - off[cur_row]));
-        cur_rows = 0;
-        cur_items = 0;
-    };
-    for (int32_t r = r0; r < r1; ++r) {
-        const int32_t d = off[r + 1] - off[r];
-        if (d > kHubRowDegree) {
-            flush();
-            const int32_t nseg = (d + kRowTileItems - 1) / kRowTileItems;
-            const int4 hub = make_int4(r, plan->nseg, nseg, 0);
-            for (int32_t s = 0; s < nseg; ++s) {
-                const int32_t b = off[r] + s * kRowTileItems;
-                plan->tiles.push_back(make_int4(r, -(plan->nseg + s + 1), b, std::min(kRowTileItems, off[r + 1] - b)));
-            }
-            plan->nseg += nseg;
-            if (nseg <= kSmallHubSegs) plan->hubs_small.push_back(hub);
-            else plan->hubs_big.push_back(hub);
-            continue;
-        }
-        if (cur_items + d + 1 > kRowTileItems) flush();
-        if (cur_rows == 0) cur_row = r;
-        ++cur_rows;
-        cur_items += d + 1;
+
+// ---- the row plan, built on the device ------------------------------------------------------------
+// Rows are tiled in fixed ranges of kPlanRange rows, one thread per range, by a greedy walk:
+// consecutive rows share a tile while their merge items (rows + nonzeros) fit in kRowTileItems, and
+// a row above kHubRowDegree becomes a hub cut into kRowTileItems segments (segments numbered from 0
+// within the range, then offset by the earlier ranges' counts). A count pass, an exclusive scan of
+// the per-range counts and a write pass produce the tiles in row order, so the plan is the same on
+// every run. Offsets that are negative, decrease or pass E stop their range's walk and set bit 4 of
+// the status flag; the walk never reads past off[V] and every write is checked against the capacity.
+constexpr int32_t kPlanRange = 2048;
+constexpr int kPlanBlock = 128;
+
+struct PlanCount {
+    int64_t tiles = 0, small = 0, big = 0, segs = 0;
+    __device__ void tile(int32_t, int32_t, int32_t, int32_t) { ++tiles; }
+    __device__ void hub(int32_t, int32_t, int32_t nseg) { (nseg <= kSmallHubSegs ? small : big) += 1; }
+};
+
+struct PlanWrite {
+    int64_t t, hs, hb, seg_base;  // next slots, and the range's first global segment id
+    int64_t cap_tiles, cap_hubs;
+    int4* tiles;
+    int4* hubs_small;
+    int4* hubs_big;
+    __device__ void tile(int32_t row, int32_t nrows_or_seg, int32_t nb, int32_t nnz) {
+        // nrows_or_seg >= 0: a normal tile of that many rows; < 0: hub segment -(local id + 1).
+        const int32_t y = nrows_or_seg >= 0 ? nrows_or_seg : static_cast<int32_t>(nrows_or_seg - seg_base);
+        if (t < cap_tiles) tiles[t] = make_int4(row, y, nb, nnz);
+        ++t;
     }
-    flush();
+    __device__ void hub(int32_t row, int32_t first_seg, int32_t nseg) {
+        const int4 h = make_int4(row, static_cast<int32_t>(seg_base + first_seg), nseg, 0);
+        if (nseg <= kSmallHubSegs) {
+            if (hs < cap_hubs) hubs_small[hs] = h;
+            ++hs;
+        } else {
+            if (hb < cap_hubs) hubs_big[hb] = h;
+            ++hb;
+        }
+    }
+};
+
+// The greedy walk over rows [r0, r1); returns the number of hub segments, or -1 on bad offsets.
+template <class Sink>
+__device__ int32_t plan_range(const int32_t* __restrict__ off, int32_t r0, int32_t r1, int64_t E, Sink& sk) {
+    int32_t cur_row = r0, cur_rows = 0, cur_items = 0, cur_nb = 0, cur_end = 0, segs = 0;
+    int32_t a = __ldg(off + r0);
+    if (a < 0 || a > E) return -1;
+    for (int32_t r = r0; r < r1; ++r) {
+        const int32_t b = __ldg(off + r + 1);
+        if (b < a || b > E) return -1;
+        const int32_t d = b - a;
+        if (d > kHubRowDegree) {
+            if (cur_rows > 0) sk.tile(cur_row, cur_rows, cur_nb, cur_end - cur_nb);
+            cur_rows = 0;
+            cur_items = 0;
+            const int32_t nseg = (d + kRowTileItems - 1) / kRowTileItems;
+            for (int32_t k = 0; k < nseg; ++k) {
+                const int32_t sb = a + k * kRowTileItems;
+                sk.tile(r, -(segs + k + 1), sb, min(kRowTileItems, b - sb));
+            }
+            sk.hub(r, segs, nseg);
+            segs += nseg;
+        } else {
+            if (cur_items + d + 1 > kRowTileItems) {
+                sk.tile(cur_row, cur_rows, cur_nb, cur_end - cur_nb);
+                cur_rows = 0;
+                cur_items = 0;
+            }
+            if (cur_rows == 0) {
+                cur_row = r;
+                cur_nb = a;
+            }
+            ++cur_rows;
+            cur_items += d + 1;
+            cur_end = b;
+        }
+        a = b;
+    }
+    if (cur_rows > 0) sk.tile(cur_row, cur_rows, cur_nb, cur_end - cur_nb);
+    return segs;
 }
+
+__device__ __forceinline__ int32_t range_end(int32_t r0, int32_t V) {
+    const int64_t end = static_cast<int64_t>(r0) + kPlanRange;
+    return static_cast<int32_t>(end < V ? end : V);
+}
+
+// counts[4][nranges]: tiles, small hubs, big hubs, segments of each range.
+__global__ void __launch_bounds__(kPlanBlock) plan_count_kernel(const int32_t* __restrict__ off, int32_t V, int64_t E,
+                                                                int64_t* __restrict__ counts, int32_t nranges, int* bad) {
+    const int32_t k = blockIdx.x * kPlanBlock + threadIdx.x;
+    if (k >= nranges) return;
+    PlanCount c;
+    const int32_t r0 = k * kPlanRange;
+    const int32_t segs = plan_range(off, r0, range_end(r0, V), E, c);
+    if (segs < 0) {
+        atomicOr(bad, 4);
+        c = PlanCount();
+    } else {
+        c.segs = segs;
+    }
+    counts[k] = c.tiles;
+    counts[nranges + k] = c.small;
+    counts[2 * static_cast<int64_t>(nranges) + k] = c.big;
+    counts[3 * static_cast<int64_t>(nranges) + k] = c.segs;
+}
+
+// In-place exclusive scan of each of the four count rows; totals[0..3] receive the sums. One block.
+__global__ void __launch_bounds__(1024) plan_scan_kernel(int64_t* counts, int32_t nranges, int64_t* totals) {
+    __shared__ int64_t s_part[4][1024];
+    const int t = threadIdx.x;
+    const int32_t per = (nranges + 1023) / 1024;
+    const int64_t lo = static_cast<int64_t>(t) * per;
+    const int64_t hi = lo + per < nranges ? lo + per : static_cast<int64_t>(nranges);
+    for (int q = 0; q < 4; ++q) {
+        int64_t acc = 0;
+        for (int64_t i = lo; i < hi; ++i) acc += counts[q * static_cast<int64_t>(nranges) + i];
+        s_part[q][t] = acc;
+    }
+    __syncthreads();
+    if (t < 4) {
+        int64_t run = 0;
+        for (int i = 0; i < 1024; ++i) {
+            const int64_t v = s_part[t][i];
+            s_part[t][i] = run;
+            run += v;
+        }
+        totals[t] = run;
+    }
+    __syncthreads();
+    for (int q = 0; q < 4; ++q) {
+        int64_t run = s_part[q][t];
+        for (int64_t i = lo; i < hi; ++i) {
+            int64_t* p = counts + q * static_cast<int64_t>(nranges) + i;
+            const int64_t v = *p;
+            *p = run;
+            run += v;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kPlanBlock) plan_write_kernel(const int32_t* __restrict__ off, int32_t V, int64_t E,
+                                                                const int64_t* __restrict__ bases, int32_t nranges,
+                                                                int4* tiles, int64_t cap_tiles, int4* hubs_small,
+                                                                int4* hubs_big, int64_t cap_hubs) {
+    const int32_t k = blockIdx.x * kPlanBlock + threadIdx.x;
+    if (k >= nranges) return;
+    PlanWrite w;
+    w.t = bases[k];
+    w.hs = bases[nranges + k];
+    w.hb = bases[2 * static_cast<int64_t>(nranges) + k];
+    w.seg_base = bases[3 * static_cast<int64_t>(nranges) + k];
+    w.cap_tiles = cap_tiles;
+    w.cap_hubs = cap_hubs;
+    w.tiles = tiles;
+    w.hubs_small = hubs_small;
+    w.hubs_big = hubs_big;
+    const int32_t r0 = k * kPlanRange;
+    plan_range(off, r0, range_end(r0, V), E, w);
+}
+
+int32_t plan_ranges(int32_t V) { return V > 0 ? static_cast<int32_t>((static_cast<int64_t>(V) + kPlanRange - 1) / kPlanRange) : 0; }
+
 }  // namespace
 
-// Rows are planned in fixed ranges of kPlanRange (independently, in parallel) and the ranges joined
-// with their hub segments renumbered, so the plan is the same whatever the thread count.
-void build_row_plan(const int32_t* off, int32_t V, RowPlanHost* plan) {
-    constexpr int32_t kPlanRange = 1 << 16;
-    const int32_t nr = V > 0 ? (V + kPlanRange - 1) / kPlanRange : 0;
-    std::vector<RowPlanHost> part(static_cast<size_t>(nr));
-#pragma omp parallel for schedule(dynamic, 1)
-    for (int32_t k = 0; k < nr; ++k)
-        plan_rows(off, k * kPlanRange, std::min(V, (k + 1) * kPlanRange), &part[k]);
-    plan->tiles.clear();
-    plan->hubs_small.clear();
-    plan->hubs_big.clear();
-    plan->nseg = 0;
-    for (RowPlanHost& p : part) {
-        const int32_t base = plan->nseg;
-        for (int4 t : p.tiles) {
-            if (t.y < 0) t.y -= base;
-            plan->tiles.push_back(t);
-        }
-        for (int4 h : p.hubs_small) plan->hubs_small.push_back(make_int4(h.x, h.y + base, h.z, h.w));
-        for (int4 h : p.hubs_big) plan->hubs_big.push_back(make_int4(h.x, h.y + base, h.z, h.w));
-        plan->nseg += p.nseg;
-    }
+// Tiles of a valid CSR: consecutive normal tiles of one run (no hub or range start between them)
+// hold more than kRowTileItems merge items per pair, so there are at most 2(V+E)/257 + runs of them;
+// a hub of degree d >= 256 gives ceil(d/256) <= d/256 + 1 segments; hubs <= E/256 and runs <=
+// hubs + ranges. Hence tiles <= (2V + 5E)/256 + ranges + 1.
+RowPlanCaps row_plan_caps(int32_t V, int64_t E) {
+    RowPlanCaps c;
+    const int64_t ranges = plan_ranges(V);
+    c.tiles = (2 * static_cast<int64_t>(V) + 5 * E) / 256 + ranges + 2;
+    c.hubs = E / 256 + 1;
+    c.scratch_bytes = sizeof(int64_t) * (4 * static_cast<size_t>(ranges > 0 ? ranges : 1) + 4);
+    return c;
+}
+
+cudaError_t launch_build_row_plan(const int32_t* off, int32_t V, int64_t E, const RowPlanCaps& caps, int4* tiles,
+                                  int4* hubs_small, int4* hubs_big, void* scratch, int64_t* totals, int* bad,
+                                  cudaStream_t s) {
+    const int32_t nr = plan_ranges(V);
+    if (nr == 0) return cudaMemsetAsync(totals, 0, 4 * sizeof(int64_t), s);
+    int64_t* counts = static_cast<int64_t*>(scratch);
+    const int blocks = (nr + kPlanBlock - 1) / kPlanBlock;
+    plan_count_kernel<<<blocks, kPlanBlock, 0, s>>>(off, V, E, counts, nr, bad);
+    plan_scan_kernel<<<1, 1024, 0, s>>>(counts, nr, totals);
+    plan_write_kernel<<<blocks, kPlanBlock, 0, s>>>(off, V, E, counts, nr, tiles, caps.tiles, hubs_small, hubs_big,
+                                                    caps.hubs);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_spmv(const RowGatherLaunch& L, DevStatus* st, cudaStream_t stream, int sm_count,

@@ -174,7 +174,8 @@ def test_one_shot_matches_graph_path_bitwise(ctx, graphs, name):
         assert np.array_equal(one.view(np.uint32), two.view(np.uint32))
 
 
-def test_one_shot_rejects_bad_columns(ctx, graphs):
+def test_one_shot_rejects_bad_input(ctx, graphs):
+    # The one-shot call checks columns and offsets on the device; the errors are the graph path's.
     g = graphs["rmat12"]
     in_off, in_col, od = _pr_inputs(g)
     for bad in (g.V, -1, 1 << 30):
@@ -184,6 +185,16 @@ def test_one_shot_rejects_bad_columns(ctx, graphs):
             dpg.pagerank_host(ctx, in_off, col, od)
         assert e.value.status == dpg.ERR_INVALID_ARG
         assert "column index out of range" in str(e.value)
+    dec = in_off.copy()
+    dec[1000] = dec[1002] + 1  # offsets decrease at vertex 1000
+    with pytest.raises(dpg.DpgError) as e:
+        dpg.pagerank_host(ctx, dec, in_col, od)
+    assert e.value.status == dpg.ERR_INVALID_ARG and "offsets decrease at vertex" in str(e.value)
+    for off in (np.concatenate([in_off[:-1], [in_off[-1] - 1]]).astype(np.int32),
+                np.concatenate([[1], in_off[1:]]).astype(np.int32)):
+        with pytest.raises(dpg.DpgError) as e:
+            dpg.pagerank_host(ctx, off, in_col, od)
+        assert e.value.status == dpg.ERR_INVALID_ARG and "offsets must start at 0 and end at E" in str(e.value)
     # The context stays usable, and the next one-shot call is right.
     r = dpg.pagerank_host(ctx, in_off, in_col, od, iterations=20)
     ref = dpg.pagerank(ctx, dpg.Graph(ctx, in_off, in_col), od, iterations=20)
