@@ -285,11 +285,21 @@ dpg_status ensure_plan(dpg_graph* g) {
     return fs;
 }
 
-// Entries of the gathered vector kept in shared memory by the row-gather kernel: as many of the
-// most frequent (renamed) columns as fit next to the tile staging.
+// Entries of the gathered vector kept in shared memory by the row-gather kernel: the most frequent
+// (renamed) columns, as many as fit next to the tile staging within a shared-memory budget of
+// DPG_GATHER_SMEM_KB per SM. The budget is below the 227 KB a CTA could take because what is left
+// of the SM's 256 KB of L1/shared memory is the L1 the scattered gathers land in: their sectors in
+// flight need L1 lines, and a 28 KB L1 (the 228 KB shared-memory carve-out) capped them well below
+// what 32 warps issue. On R-MAT scale 22 a PageRank sweep took 0.29 ms with every free byte given
+// to the hot cache (31.5 K entries) and 0.202 ms at this budget (16 K entries, 92 KB of L1).
+#ifndef DPG_GATHER_SMEM_KB
+#define DPG_GATHER_SMEM_KB 164
+#endif
 int32_t hot_entries(const dpg_ctx* c, const dpg_graph* g) {
     if (!g->relabel) return 0;
-    const int64_t room = static_cast<int64_t>(c->smem_optin) - static_cast<int64_t>(rowgather_staging_bytes()) - 1024;
+    // 1 KB of each carve-out is reserved per CTA by the system.
+    const int64_t budget = std::min<int64_t>(c->smem_optin, DPG_GATHER_SMEM_KB * 1024 - 1024);
+    const int64_t room = budget - static_cast<int64_t>(rowgather_staging_bytes());
     const int64_t cap = room > 0 ? room / 4 : 0;
     return static_cast<int32_t>(cap < g->V ? cap : g->V);
 }

@@ -28,21 +28,27 @@
 namespace dpg {
 namespace {
 
-// One 1024-thread CTA per SM: its dynamic shared memory holds the hot-value cache (the first
-// `hot` renamed entries of x, i.e. the most gathered columns) and the 32 warps' tile staging.
-constexpr int kBlock = 1024;
+// One CTA per SM: its dynamic shared memory holds the hot-value cache (the first `hot` renamed
+// entries of x, i.e. the most gathered columns) and its warps' tile staging.
+#ifndef DPG_GATHER_BLOCK
+#define DPG_GATHER_BLOCK 1024
+#endif
+constexpr int kBlock = DPG_GATHER_BLOCK;
 constexpr int kWarps = kBlock / 32;
 constexpr int kInitBlock = 256;
 constexpr int kIpl = kRowTileItems / 32;  // merge items per lane
 constexpr int kFixBlock = 256;
 // Tiles a warp carries through one step (see rowgather_kernel), per mode. Measured on R-MAT scale
-// 22 with the next step's descriptors prefetched: PageRank runs best with 1 (0.29 ms per sweep;
-// at 3 its registers spill), SpMV with 2 (145.5 GTEPS against 139.8 with 3, which spills).
+// 22 (PageRank sweep, 1024-thread CTAs): what limits the gathers is the L1 left beside the shared
+// memory, where their sectors in flight need lines (the shared-memory budget is set with the
+// hot-cache size, see hot_entries). With a 28 KB L1 one tile per step ran best (0.29 ms per sweep);
+// with 92 KB, two tiles run 0.202 ms against 0.216 ms with one. Fewer warps lose at any setting
+// (768 threads: 0.245 ms, 512: 0.35 ms), and three tiles would spill at 1024 threads.
 #ifndef DPG_GATHER_TILES_SPMV
 #define DPG_GATHER_TILES_SPMV 2
 #endif
 #ifndef DPG_GATHER_TILES_PR
-#define DPG_GATHER_TILES_PR 1
+#define DPG_GATHER_TILES_PR 2
 #endif
 // Shared-memory index with one pad word per 32: lane l walking items 8l.. then hits 32 distinct banks
 // instead of 4 (an 8-way conflict without the pad).
