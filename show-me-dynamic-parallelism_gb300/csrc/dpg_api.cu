@@ -194,7 +194,7 @@ void graph_free_device(dpg_graph* g) {
     g->spmm_ready = g->spmm_t_ready = false;
     g->relabel_ready = false;
     dev_free(g->ctx, g->plan.tiles);
-    dev_free(g->ctx, g->plan.lane_r0);
+    dev_free(g->ctx, g->plan.lane_info);
     dev_free(g->ctx, g->plan.hubs_small);
     dev_free(g->ctx, g->plan.hubs_big);
     g->off = nullptr;
@@ -240,7 +240,7 @@ dpg_status plan_finish(dpg_graph* g, PlanBuild* pb, const PlanInfo& info) {
     d.nhub_big = static_cast<int32_t>(nbg);
     d.nseg = static_cast<int32_t>(nsg);
     DPG_CUDA_TRY(dev_alloc(c, &d.tiles, sizeof(int4) * static_cast<size_t>(nt + 1)));
-    DPG_CUDA_TRY(dev_alloc(c, &d.lane_r0, 32 * static_cast<size_t>(nt + 1)));
+    DPG_CUDA_TRY(dev_alloc(c, &d.lane_info, 32 * sizeof(uint16_t) * static_cast<size_t>(nt + 1)));
     DPG_CUDA_TRY(dev_alloc(c, &d.hubs_small, sizeof(int4) * static_cast<size_t>(nsm + 1)));
     DPG_CUDA_TRY(dev_alloc(c, &d.hubs_big, sizeof(int4) * static_cast<size_t>(nbg + 1)));
     if (nt > 0)

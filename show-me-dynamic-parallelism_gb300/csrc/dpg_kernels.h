@@ -139,7 +139,9 @@ cudaError_t launch_build_row_plan(const int32_t* off, int32_t V, int64_t E, cons
 
 struct RowPlanDev {
     int4* tiles = nullptr;
-    uint8_t* lane_r0 = nullptr;  // [ntiles][32] merge-path start row of each lane (normal tiles)
+    // [ntiles][32] per lane of a normal tile: merge-path start row (low byte) and the mask of its
+    // merge items that are row ends (high byte, bit i = item 8*lane + i).
+    uint16_t* lane_info = nullptr;
     int32_t ntiles = 0;
     int4* hubs_small = nullptr;
     int32_t nhub_small = 0;
@@ -282,7 +284,7 @@ size_t frequency_order_scratch_bytes(int32_t V);
 cudaError_t launch_frequency_order(const int32_t* counts, int32_t V, int32_t* scratch, int32_t* perm, int32_t* inv,
                                    cudaStream_t s);
 
-// Fills plan.lane_r0 from the tiles and the offsets (once per graph).
+// Fills plan.lane_info from the tiles and the offsets (once per graph).
 cudaError_t launch_tile_lane_starts(const RowPlanDev& plan, const int32_t* off, cudaStream_t s, int sm_count);
 
 // Grid shape used by the row-gather kernels (needed to size dpart/dfix).

@@ -92,9 +92,9 @@ __device__ __forceinline__ float pr_base(const RowGatherLaunch& L) {
     return static_cast<float>(L.base_const + L.dangling_scale * __ldg(L.dsum_in));
 }
 
-// One step of a warp covers KT consecutive tiles: first every column, row-end and epilogue load of
-// all KT tiles, then all their gathers, then the tiles are walked one after the other through the
-// warp's single staging area. A lane thus keeps KT x 8 gathers in flight instead of 8.
+// One step of a warp covers KT consecutive tiles: first every column and epilogue load of all KT
+// tiles, then all their gathers, then the tiles are walked one after the other through the warp's
+// single staging area. A lane thus keeps KT x 8 gathers in flight instead of 8.
 template <int MODE, int KT>
 __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
     extern __shared__ __align__(16) unsigned char rg_smem[];
@@ -102,10 +102,9 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
     const int lane = threadIdx.x & 31;
     const int gwarp = blockIdx.x * kWarps + warp;
     const int nwarps = gridDim.x * kWarps;
-    int* re = reinterpret_cast<int*>(rg_smem) + warp * (3 * kPadded);
-    float* val = reinterpret_cast<float*>(re + kPadded);
+    float* val = reinterpret_cast<float*>(rg_smem) + warp * (2 * kPadded);
     float* out = val + kPadded;
-    float* s_hot = reinterpret_cast<float*>(rg_smem) + kWarps * 3 * kPadded;
+    float* s_hot = reinterpret_cast<float*>(rg_smem) + kWarps * 2 * kPadded;
     for (int i = threadIdx.x; i < L.hot; i += kBlock) s_hot[i] = __ldg(L.x + i);
     __syncthreads();
     float base = 0.0f;
@@ -113,32 +112,31 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
     double dang = 0.0;
 
     const int ntiles = L.plan.ntiles;
-    // Descriptors and lane starts of the next step are requested one step ahead.
+    // Descriptors and lane walks of the next step are requested one step ahead.
     int4 Tn[KT];
-    int r0n[KT];
+    int infon[KT];
 #pragma unroll
     for (int k = 0; k < KT; ++k) {
         const int t = gwarp * KT + k;
         Tn[k] = t < ntiles ? __ldg(L.plan.tiles + t) : make_int4(0, 0, 0, 0);
-        r0n[k] = t < ntiles ? __ldg(L.plan.lane_r0 + t * 32 + lane) : 0;
+        infon[k] = t < ntiles ? __ldg(L.plan.lane_info + t * 32 + lane) : 0;
     }
     for (int t0 = gwarp * KT; t0 < ntiles; t0 += nwarps * KT) {
         int4 T[KT];
-        int r0[KT], re0[KT], od0[KT], pos0[KT];
+        int info[KT], od0[KT], pos0[KT];
         float pv[KT][kIpl];
-        // Phase 1: columns, the first 32 row ends and epilogue inputs of every tile.
+        // Phase 1: columns and the epilogue inputs of the first 32 rows of every tile.
         int cols[KT][kIpl];
 #pragma unroll
         for (int k = 0; k < KT; ++k) {
             T[k] = Tn[k];
-            r0[k] = r0n[k];
+            info[k] = infon[k];
             const int row = T[k].x, nrows = T[k].y, nb = T[k].z, nnz = T[k].w;
 #pragma unroll
             for (int i = 0; i < kIpl; ++i) {
                 const int j = i * 32 + lane;
                 cols[k][i] = j < nnz ? __ldg(L.col + nb + j) : 0;
             }
-            re0[k] = lane < nrows ? __ldg(L.off + row + lane + 1) - nb : 0;
             od0[k] = 0;
             pos0[k] = 0;
             if (MODE == kModePagerank && lane < nrows) {
@@ -150,7 +148,7 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
         for (int k = 0; k < KT; ++k) {
             const int t = t0 + nwarps * KT + k;
             Tn[k] = t < ntiles ? __ldg(L.plan.tiles + t) : make_int4(0, 0, 0, 0);
-            r0n[k] = t < ntiles ? __ldg(L.plan.lane_r0 + t * 32 + lane) : 0;
+            infon[k] = t < ntiles ? __ldg(L.plan.lane_info + t * 32 + lane) : 0;
         }
         // Phase 2: the gathers of every tile.
 #pragma unroll
@@ -182,29 +180,27 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
                 if (lane == 0) L.partial[-(nrows + 1)] = acc;
                 continue;
             }
-            if (lane < nrows) re[pad(lane)] = re0[k];
-            for (int r = lane + 32; r < nrows; r += 32) re[pad(r)] = __ldg(L.off + row + r + 1) - nb;
 #pragma unroll
             for (int i = 0; i < kIpl; ++i) {
                 const int j = i * 32 + lane;
                 if (j < nnz) val[pad(j)] = pv[k][i];
             }
             __syncwarp();
-            // Merge-path: lane owns merge items [d0, d1) starting at row r0 (precomputed per tile);
+            // Merge-path: lane owns merge items [d0, d1) starting at row r0; the plan's mask says
+            // which of them are row ends (emit the open row) and which are nonzeros (take one).
             // r = row ends consumed, kk = nonzeros consumed. The walk is branch-free.
             const int total = nrows + nnz;
             const int d0 = min(lane * kIpl, total);
-            const int d1 = min(d0 + kIpl, total);
-            int r = d0 < total ? r0[k] : nrows;
+            const int nlive = min(d0 + kIpl, total) - d0;
+            const unsigned ends = static_cast<unsigned>(info[k]) >> 8;
+            int r = d0 < total ? (info[k] & 0xFF) : nrows;
             int kk = d0 - r;
             float acc = 0.0f;
             int first_emit = -1;
-            int rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
 #pragma unroll
             for (int i = 0; i < kIpl; ++i) {
-                const bool live = d0 + i < d1;
-                const bool take = live && kk < rend;
-                const bool emit = live && !(kk < rend);
+                const bool emit = (ends >> i) & 1u;
+                const bool take = i < nlive && !emit;
                 const float v = val[pad(kk)];  // kk <= nnz <= 255 stays inside the padded row
                 if (emit) {
                     out[pad(r)] = acc;
@@ -213,7 +209,6 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
                 acc = take ? acc + v : (emit ? 0.0f : acc);
                 kk += take ? 1 : 0;
                 r += emit ? 1 : 0;
-                if (emit) rend = r < nrows ? re[pad(r)] : 0x7FFFFFFF;
             }
             // Segmented inclusive scan of the lanes' open partials (key = row still open at lane end).
             float cv = acc;
@@ -321,16 +316,19 @@ __global__ void __launch_bounds__(kInitBlock) pr_init_kernel(RowGatherLaunch L, 
     if (lane == 0) L.dpart[gwarp] = dang;
 }
 
-// Merge-path start row of each lane of each normal tile, once per graph: the largest r with
-// (row end r-1) + r <= 8 * lane, i.e. the row ends the lane's first merge item comes after.
+// Per lane of each normal tile, once per graph: the merge-path start row, i.e. the largest r with
+// (row end r-1) + r <= 8 * lane (the row ends the lane's first merge item comes after), and which
+// of the lane's 8 merge items are row ends rather than nonzeros. With both, the gather kernel walks
+// its items without reading any row end.
 __global__ void tile_lane_starts_kernel(const int4* __restrict__ tiles, int ntiles, const int32_t* __restrict__ off,
-                                        uint8_t* __restrict__ lane_r0) {
+                                        uint16_t* __restrict__ lane_info) {
     const int lane = threadIdx.x & 31;
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int t = w; t < ntiles; t += nw) {
         const int4 T = __ldg(tiles + t);
         int lo = 0;
+        unsigned ends = 0;
         if (T.y > 0) {
             const int row = T.x, nrows = T.y, nb = T.z, nnz = T.w;
             const int total = nrows + nnz;
@@ -342,15 +340,29 @@ __global__ void tile_lane_starts_kernel(const int4* __restrict__ tiles, int ntil
                 if (__ldg(off + row + mid) - nb + mid <= d0) lo = mid;
                 else hi = mid - 1;
             }
+            // The lane's items in merge order: nonzero kk while kk < (end of row r), else the end of r.
+            int r = lo, kk = d0 - lo;
+            const int d1 = min(d0 + kIpl, total);
+            int rend = r < nrows ? __ldg(off + row + r + 1) - nb : 0x7FFFFFFF;
+            for (int i = 0; d0 + i < d1; ++i) {
+                if (kk < rend) {
+                    ++kk;
+                } else {
+                    ends |= 1u << i;
+                    ++r;
+                    rend = r < nrows ? __ldg(off + row + r + 1) - nb : 0x7FFFFFFF;
+                }
+            }
         }
-        lane_r0[static_cast<int64_t>(t) * 32 + lane] = static_cast<uint8_t>(lo > 255 ? 255 : lo);
+        lane_info[static_cast<int64_t>(t) * 32 + lane] = static_cast<uint16_t>(lo | (ends << 8));
     }
 }
 
 }  // namespace
 
 cudaError_t launch_tile_lane_starts(const RowPlanDev& plan, const int32_t* off, cudaStream_t s, int sm_count) {
-    if (plan.ntiles > 0) tile_lane_starts_kernel<<<sm_count * 8, 256, 0, s>>>(plan.tiles, plan.ntiles, off, plan.lane_r0);
+    if (plan.ntiles > 0)
+        tile_lane_starts_kernel<<<sm_count * 8, 256, 0, s>>>(plan.tiles, plan.ntiles, off, plan.lane_info);
     return cudaGetLastError();
 }
 
@@ -360,7 +372,7 @@ void rowgather_grid(int sm_count, int* gather_blocks, int* fix_blocks, int* bloc
     *block_threads = kBlock;
 }
 
-size_t rowgather_staging_bytes() { return sizeof(int) * kWarps * 3 * kPadded; }
+size_t rowgather_staging_bytes() { return sizeof(int) * kWarps * 2 * kPadded; }
 
 namespace {
 
