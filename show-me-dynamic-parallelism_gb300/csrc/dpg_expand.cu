@@ -77,11 +77,15 @@ struct ExpandParams {
 //   load_edge(e, rv)       label index v, adjacency row r and candidate value of arc e's head
 //   want(v, cand, cur)     cheap filter before the atomic (cur = label[v] when kPeek)
 //   commit(v, cand)        the atomic update; true when v must be pushed
+//   kMinBlocks             CTAs per SM the kernel is compiled for (its register budget); measured on
+//                          R-MAT scale 24: 3 CTAs (85 registers) solve SSSP in 8.64 ms against 9.31 ms
+//                          with the 2 that 111 registers allow; at 4 the registers spill.
 struct SsspOp {
     using RV = int;
     static constexpr bool kDedup = true;
     static constexpr bool kPeek = true;
     static constexpr bool kMask = false;
+    static constexpr int kMinBlocks = 3;
     __device__ __forceinline__ static int row_value(const ExpandParams& P, int u, int) { return __ldcg(P.label + u); }
     __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v, int& r,
                                                      int& cand) {
@@ -103,6 +107,7 @@ struct BfsOp {
     static constexpr bool kDedup = false;
     static constexpr bool kPeek = true;
     static constexpr bool kMask = false;
+    static constexpr int kMinBlocks = 3;
     __device__ __forceinline__ static int row_value(const ExpandParams& P, int u, int) { return __ldcg(P.label + u); }
     __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v, int& r,
                                                      int& cand) {
@@ -124,6 +129,7 @@ struct ColorOp {
     static constexpr bool kDedup = false;
     static constexpr bool kPeek = false;
     static constexpr bool kMask = false;
+    static constexpr int kMinBlocks = 3;
     __device__ __forceinline__ static int row_value(const ExpandParams&, int u, int) { return u; }
     __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int u, int& v, int& r, int& cand) {
         v = __ldg(P.col + e);
@@ -149,6 +155,7 @@ struct MaskSsspOp {
     using RV = int2;  // {vertex, source mask}
     static constexpr bool kDedup = false;
     static constexpr bool kMask = true;
+    static constexpr int kMinBlocks = 1;
     __device__ __forceinline__ static int2 row_value(const ExpandParams& P, int u, int j) {
         const unsigned long long w = __ldcg(P.dirty[j & 1] + u);
         const unsigned mask = (w >> 32) == static_cast<unsigned long long>(static_cast<unsigned>(j))
@@ -491,7 +498,7 @@ __device__ __forceinline__ void warp_row(const ExpandParams& P, const PushCtx& Q
 }
 
 template <class Op, int POL, int CH = kHubChunk>
-__global__ void __launch_bounds__(kBlock) expand_kernel(ExpandParams P) {
+__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) expand_kernel(ExpandParams P) {
     using RV = typename Op::RV;
     constexpr bool kDirOpt = (POL == DPG_SOL_DIROPT);
     constexpr bool kNearFar = (POL == DPG_SOL_NEARFAR);
