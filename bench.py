@@ -14,7 +14,8 @@ dangling mass spread uniformly) over a seeded R-MAT graph of scale 22 and edge f
   CUDA events recorded around every launch inside the timed region.
 * cpu_baseline / --impl reference: the CPU restatement of the reference's PageRank (the reference
   has no CPU PageRank), all host threads, timed on a bounded sample.
-* extra: SpMV on the same graph, SSSP and BFS on R-MAT scale 24 (268,435,456 arcs).
+* extra: SpMV on the same graph; SSSP, BFS and PageRank on R-MAT scale 24 (268,435,456 arcs); the
+  adjoint, gradient, batch, grid and CDP2 legs.
 Multi-GPU (torchrun): replicas only, one independent copy of the workload per rank; time = max over
 ranks; value = all ranks' arcs x sweeps / that time.
 """
@@ -558,15 +559,59 @@ def measure_grid(dpg, ctx, torch, peak, n=4096, nsrc=2):
             f"bfs_grid{n}": measure_expand(dpg, ctx, torch, g, peak, "bfs", nsrc=nsrc)}
 
 
+def measure_pagerank_large(dpg, ctx, torch, g, peak, steps=5):
+    """20-sweep pull PageRank (d = 0.85) on a large graph, device-resident: the in-edge CSR is built
+    on the device (invertGraph order), the sweeps are timed with CUDA events, and the gather kernel's
+    average launch gives the roofline fraction. rank_sum (1 up to rounding) is a size-independent
+    check of the result."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    V, E = g.V, g.E
+    off = torch.from_numpy(g.offsets).to(dev)
+    col = torch.from_numpy(g.col).to(dev)
+    in_off = torch.empty(V + 1, dtype=torch.int32, device=dev)
+    in_col = torch.empty(E, dtype=torch.int32, device=dev)
+    dpg.csr_transpose_dev(ctx, V, E, off.data_ptr(), col.data_ptr(), in_off.data_ptr(), in_col.data_ptr())
+    od = (off[1:] - off[:-1]).to(torch.int32).contiguous()
+    ctx.synchronize()
+    del col
+    gi = dpg.Graph.from_device(ctx, V, E, in_off.data_ptr(), in_col.data_ptr())
+    del in_col
+    rank = torch.empty(V, dtype=torch.float32, device=dev)
+    for _ in range(2):
+        dpg.pagerank_dev(ctx, gi, od.data_ptr(), rank.data_ptr(), damping=DAMPING, iterations=SWEEPS)
+    ctx.synchronize()
+    ctx.profile(True)
+    ctx.profile_reset()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        dpg.pagerank_dev(ctx, gi, od.data_ptr(), rank.data_ptr(), damping=DAMPING, iterations=SWEEPS)
+    e1.record()
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    n_g, ms_g = ctx.profile_read(dpg.KERNEL_ROWGATHER)
+    ctx.profile(False)
+    t_ms = e0.elapsed_time(e1) / steps
+    gather_ms = ms_g / max(n_g, 1)
+    bytes_sweep = 4 * (V + 1) + 4 * E + 12 * V
+    achieved = bytes_sweep / (gather_ms / 1e3) / 1e9
+    out = {"gteps": E * SWEEPS / (t_ms / 1e3) / 1e9, "ms_per_solve": t_ms, "sweeps": SWEEPS,
+           "gather_ms_per_sweep": gather_ms, "roofline_frac": achieved / peak, "bytes_per_sweep": bytes_sweep,
+           "rank_sum": float(rank.double().sum().item())}
+    del gi
+    return out
+
+
 def extra_measurements(dpg, ctx, torch, g, peak, steps):
-    """SpMV and the SpMV adjoint on the scale-22 graph; SSSP and BFS on R-MAT scale 24; the PageRank
-    edge-weight gradient on scale 20; the 512-graph batch; the recursive CDP2 BFS variants against
+    """SpMV and the SpMV adjoint on the scale-22 graph; SSSP, BFS and PageRank on R-MAT scale 24; the
+    PageRank edge-weight gradient on scale 20; the 512-graph batch; the recursive CDP2 BFS variants against
     the persistent BFS on scale 16 (device-resident, CUDA events)."""
     out = {"spmv_rmat22": measure_spmv(dpg, ctx, torch, g, peak, steps)}
     out["spmv_bwd_rmat22_64rhs"] = measure_adjoint(dpg, ctx, torch, g, peak)
     g24 = dpg.rmat_csr(24, 16, seed=24, wmin=1, wmax=255)
     out["sssp_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "sssp")
     out["bfs_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "bfs")
+    out["pagerank_rmat24"] = measure_pagerank_large(dpg, ctx, torch, g24, peak)
     out.update(measure_grid(dpg, ctx, torch, peak))
     del g24
     g20 = dpg.rmat_csr(20, 16, seed=20, weights=False)

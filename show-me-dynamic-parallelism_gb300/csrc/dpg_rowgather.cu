@@ -38,6 +38,7 @@ constexpr int kWarps = kBlock / 32;
 constexpr int kInitBlock = 256;
 constexpr int kIpl = kRowTileItems / 32;  // merge items per lane
 constexpr int kFixBlock = 256;
+constexpr int kFixBatch = 8;  // loads the fix-up issues before it adds them
 // Tiles a warp carries through one step (see rowgather_kernel), per mode. Measured on R-MAT scale
 // 22 (PageRank sweep, 1024-thread CTAs): what limits the gathers is the L1 left beside the shared
 // memory, where their sectors in flight need lines (the shared-memory budget is set with the
@@ -255,17 +256,29 @@ __global__ void __launch_bounds__(kFixBlock) hub_fixup_kernel(RowGatherLaunch L,
     float base = 0.0f;
     if (MODE == kModePagerank) base = pr_base(L);
     double dang = 0.0;
+    // Every loop below issues its loads in batches before adding them in the same order as a plain
+    // loop would, so the sums are unchanged and each batch costs one memory round trip.
     for (int h = tid; h < L.plan.nhub_small; h += nthreads) {
         const int4 H = __ldg(L.plan.hubs_small + h);
+        float p[kSmallHubSegs];
+#pragma unroll
+        for (int s = 0; s < kSmallHubSegs; ++s) p[s] = s < H.z ? L.partial[H.y + s] : 0.0f;
         float acc = 0.0f;
-        for (int s = 0; s < H.z; ++s) acc += L.partial[H.y + s];
+#pragma unroll
+        for (int s = 0; s < kSmallHubSegs; ++s) acc += p[s];
         if (MODE == kModeSpmv) L.y[H.x] = acc;
         else pr_epilogue(L, H.x, acc, base, dang);
     }
     for (int h = gwarp; h < L.plan.nhub_big; h += nwarps) {
         const int4 H = __ldg(L.plan.hubs_big + h);
         float acc = 0.0f;
-        for (int s = lane; s < H.z; s += 32) acc += L.partial[H.y + s];
+        for (int s0 = lane; s0 < H.z; s0 += 32 * kFixBatch) {
+            float p[kFixBatch];
+#pragma unroll
+            for (int q = 0; q < kFixBatch; ++q) p[q] = s0 + 32 * q < H.z ? L.partial[H.y + s0 + 32 * q] : 0.0f;
+#pragma unroll
+            for (int q = 0; q < kFixBatch; ++q) acc += p[q];
+        }
         acc = warp_sum_f32(acc);
         if (lane == 0) {
             if (MODE == kModeSpmv) L.y[H.x] = acc;
@@ -283,8 +296,20 @@ __global__ void __launch_bounds__(kFixBlock) hub_fixup_kernel(RowGatherLaunch L,
     if (!s_last) return;
     __threadfence();
     double acc = 0.0;
-    for (int i = threadIdx.x; i < gather_warps; i += blockDim.x) acc += __ldcg(L.dpart + i);
-    for (int i = threadIdx.x; i < nwarps; i += blockDim.x) acc += __ldcg(L.dfix + i);
+    for (int i0 = threadIdx.x; i0 < gather_warps; i0 += kFixBlock * kFixBatch) {
+        double p[kFixBatch];
+#pragma unroll
+        for (int q = 0; q < kFixBatch; ++q) p[q] = i0 + kFixBlock * q < gather_warps ? __ldcg(L.dpart + i0 + kFixBlock * q) : 0.0;
+#pragma unroll
+        for (int q = 0; q < kFixBatch; ++q) acc += p[q];
+    }
+    for (int i0 = threadIdx.x; i0 < nwarps; i0 += kFixBlock * kFixBatch) {
+        double p[kFixBatch];
+#pragma unroll
+        for (int q = 0; q < kFixBatch; ++q) p[q] = i0 + kFixBlock * q < nwarps ? __ldcg(L.dfix + i0 + kFixBlock * q) : 0.0;
+#pragma unroll
+        for (int q = 0; q < kFixBatch; ++q) acc += p[q];
+    }
     __shared__ double s_red[kFixBlock / 32];
     acc = warp_sum_f64(acc);
     if (lane == 0) s_red[threadIdx.x >> 5] = acc;
