@@ -77,15 +77,17 @@ struct ExpandParams {
 //   load_edge(e, rv)       label index v, adjacency row r and candidate value of arc e's head
 //   want(v, cand, cur)     cheap filter before the atomic (cur = label[v] when kPeek)
 //   commit(v, cand)        the atomic update; true when v must be pushed
-//   kMinBlocks             CTAs per SM the kernel is compiled for (its register budget); measured on
-//                          R-MAT scale 24: 3 CTAs (85 registers) solve SSSP in 8.64 ms against 9.31 ms
-//                          with the 2 that 111 registers allow; at 4 the registers spill.
+//   min_blocks(CH)         CTAs per SM the kernel is compiled for (its register budget). A bound is
+//                          always given: without one the compiler picks its own, and an explicit 1
+//                          lets it spend up to 110 registers where it would otherwise use 64.
+//                          Single-source SSSP on R-MAT scale 24 takes 8.6-9.1 ms at 3 CTAs (80
+//                          registers) against 9.3 ms at 2; at 4 the registers spill.
 struct SsspOp {
     using RV = int;
     static constexpr bool kDedup = true;
     static constexpr bool kPeek = true;
     static constexpr bool kMask = false;
-    static constexpr int kMinBlocks = 3;
+    static constexpr int min_blocks(int) { return 3; }
     __device__ __forceinline__ static int row_value(const ExpandParams& P, int u, int) { return __ldcg(P.label + u); }
     __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v, int& r,
                                                      int& cand) {
@@ -107,7 +109,7 @@ struct BfsOp {
     static constexpr bool kDedup = false;
     static constexpr bool kPeek = true;
     static constexpr bool kMask = false;
-    static constexpr int kMinBlocks = 3;
+    static constexpr int min_blocks(int) { return 3; }
     __device__ __forceinline__ static int row_value(const ExpandParams& P, int u, int) { return __ldcg(P.label + u); }
     __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v, int& r,
                                                      int& cand) {
@@ -129,7 +131,7 @@ struct ColorOp {
     static constexpr bool kDedup = false;
     static constexpr bool kPeek = false;
     static constexpr bool kMask = false;
-    static constexpr int kMinBlocks = 3;
+    static constexpr int min_blocks(int) { return 3; }
     __device__ __forceinline__ static int row_value(const ExpandParams&, int u, int) { return u; }
     __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int u, int& v, int& r, int& cand) {
         v = __ldg(P.col + e);
@@ -155,7 +157,9 @@ struct MaskSsspOp {
     using RV = int2;  // {vertex, source mask}
     static constexpr bool kDedup = false;
     static constexpr bool kMask = true;
-    static constexpr int kMinBlocks = 1;
+    // 64 registers (4 CTAs) with 128- and 256-arc chunks, 128 (2 CTAs) with 512: the batch autotuner
+    // compares the three.
+    static constexpr int min_blocks(int ch) { return ch >= 512 ? 2 : 4; }
     __device__ __forceinline__ static int2 row_value(const ExpandParams& P, int u, int j) {
         const unsigned long long w = __ldcg(P.dirty[j & 1] + u);
         const unsigned mask = (w >> 32) == static_cast<unsigned long long>(static_cast<unsigned>(j))
@@ -498,7 +502,7 @@ __device__ __forceinline__ void warp_row(const ExpandParams& P, const PushCtx& Q
 }
 
 template <class Op, int POL, int CH = kHubChunk>
-__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) expand_kernel(ExpandParams P) {
+__global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(ExpandParams P) {
     using RV = typename Op::RV;
     constexpr bool kDirOpt = (POL == DPG_SOL_DIROPT);
     constexpr bool kNearFar = (POL == DPG_SOL_NEARFAR);
