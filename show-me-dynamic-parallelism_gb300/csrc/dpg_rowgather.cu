@@ -99,8 +99,14 @@ __device__ __forceinline__ float pr_base(const RowGatherLaunch& L) {
 template <int MODE>
 __device__ __forceinline__ void fixup_hubs(const RowGatherLaunch& L, int tid, int nthreads, int gwarp, int nwarps,
                                            int lane, float base, double& dang) {
+    // The epilogue inputs (out-degree, contribution slot) are loaded with the partials.
     for (int h = tid; h < L.plan.nhub_small; h += nthreads) {
         const int4 H = __ldg(L.plan.hubs_small + h);
+        int od = 0, pos = 0;
+        if (MODE == kModePagerank) {
+            od = __ldg(L.outdeg + H.x);
+            pos = L.perm ? __ldg(L.perm + H.x) : H.x;
+        }
         float p[kSmallHubSegs];
 #pragma unroll
         for (int s = 0; s < kSmallHubSegs; ++s) p[s] = s < H.z ? L.partial[H.y + s] : 0.0f;
@@ -108,10 +114,15 @@ __device__ __forceinline__ void fixup_hubs(const RowGatherLaunch& L, int tid, in
 #pragma unroll
         for (int s = 0; s < kSmallHubSegs; ++s) acc += p[s];
         if (MODE == kModeSpmv) L.y[H.x] = acc;
-        else pr_epilogue(L, H.x, acc, base, dang);
+        else pr_epilogue(L, H.x, acc, base, od, pos, dang);
     }
     for (int h = gwarp; h < L.plan.nhub_big; h += nwarps) {
         const int4 H = __ldg(L.plan.hubs_big + h);
+        int od = 0, pos = 0;
+        if (MODE == kModePagerank && lane == 0) {
+            od = __ldg(L.outdeg + H.x);
+            pos = L.perm ? __ldg(L.perm + H.x) : H.x;
+        }
         float acc = 0.0f;
         for (int s0 = lane; s0 < H.z; s0 += 32 * kFixBatch) {
             float p[kFixBatch];
@@ -123,7 +134,7 @@ __device__ __forceinline__ void fixup_hubs(const RowGatherLaunch& L, int tid, in
         acc = warp_sum_f32(acc);
         if (lane == 0) {
             if (MODE == kModeSpmv) L.y[H.x] = acc;
-            else pr_epilogue(L, H.x, acc, base, dang);
+            else pr_epilogue(L, H.x, acc, base, od, pos, dang);
         }
     }
 }
@@ -264,16 +275,14 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
             int r = d0 < total ? (info[k] & 0xFF) : nrows;
             int kk = d0 - r;
             float acc = 0.0f;
-            int first_emit = -1;
+            // Rows advance only at row ends, so the first row the lane closes is its start row.
+            const int first_emit = ends != 0u ? r : -1;
 #pragma unroll
             for (int i = 0; i < kIpl; ++i) {
                 const bool emit = (ends >> i) & 1u;
                 const bool take = i < nlive && !emit;
                 const float v = val[pad(kk)];  // kk <= nnz <= 255 stays inside the padded row
-                if (emit) {
-                    out[pad(r)] = acc;
-                    first_emit = first_emit < 0 ? r : first_emit;
-                }
+                if (emit) out[pad(r)] = acc;
                 acc = take ? acc + v : (emit ? 0.0f : acc);
                 kk += take ? 1 : 0;
                 r += emit ? 1 : 0;
