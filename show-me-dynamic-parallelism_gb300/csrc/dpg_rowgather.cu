@@ -178,7 +178,15 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
     float* val = reinterpret_cast<float*>(rg_smem) + warp * (2 * kPadded);
     float* out = val + kPadded;
     float* s_hot = reinterpret_cast<float*>(rg_smem) + kWarps * 2 * kPadded;
-    for (int i = threadIdx.x; i < L.hot; i += kBlock) s_hot[i] = __ldg(L.x + i);
+    // Hot-cache fill, loads issued in batches of 8 (one round trip each instead of one per entry).
+    for (int i0 = threadIdx.x; i0 < L.hot; i0 += kBlock * 8) {
+        float h[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) h[q] = i0 + kBlock * q < L.hot ? __ldg(L.x + i0 + kBlock * q) : 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (i0 + kBlock * q < L.hot) s_hot[i0 + kBlock * q] = h[q];
+    }
     __syncthreads();
     float base = 0.0f;
     if (MODE == kModePagerank) base = pr_base(L);
@@ -321,9 +329,8 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
     }
 }
 
-// The hub fix-up as a kernel of its own, when the gather runs without it (no cooperative launch)
-// and after the initial vector. For PageRank the last CTA to finish also reduces every dangling
-// partial (gather warps, then fix-up warps, in index order) into dsum_out.
+// The hub fix-up after each gather launch (and, with no hubs, after the initial vector). For
+// PageRank it also reduces the sweep's dangling mass into dsum_out.
 template <int MODE>
 __global__ void __launch_bounds__(kFixBlock) hub_fixup_kernel(RowGatherLaunch L, int gather_warps, DevStatus* st) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -336,18 +343,24 @@ __global__ void __launch_bounds__(kFixBlock) hub_fixup_kernel(RowGatherLaunch L,
     double dang = 0.0;
     fixup_hubs<MODE>(L, tid, nthreads, gwarp, nwarps, lane, base, dang);
     if (MODE != kModePagerank) return;
-    dang = warp_sum_f64(dang);
-    if (lane == 0) L.dfix[gwarp] = dang;
-    __threadfence();
-    __syncthreads();
+    // Block b adds its slice of the gather warps' dangling partials to its own rows' (slices in
+    // index order), leaves one partial, and the last block to finish adds those in block order.
+    const int per = (gather_warps + gridDim.x - 1) / gridDim.x;
+    const int lo = min(gather_warps, static_cast<int>(blockIdx.x) * per);
+    const int hi = min(gather_warps, lo + per);
+    double slice = 0.0;
+    for (int i = lo + static_cast<int>(threadIdx.x); i < hi; i += kFixBlock) slice += __ldcg(L.dpart + i);
+    const double bsum = block_sum_f64<kFixBlock>(slice + dang);
     __shared__ int s_last;
-    if (threadIdx.x == 0) s_last = atomicAdd(&st->fix_count, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) {
+        L.dfix[blockIdx.x] = bsum;
+        __threadfence();
+        s_last = atomicAdd(&st->fix_count, 1u) == gridDim.x - 1;
+    }
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    double acc = strided_sum_f64<kFixBlock>(L.dpart, gather_warps, 0.0);
-    acc = strided_sum_f64<kFixBlock>(L.dfix, nwarps, acc);
-    const double total = block_sum_f64<kFixBlock>(acc);
+    const double total = block_sum_f64<kFixBlock>(strided_sum_f64<kFixBlock>(L.dfix, gridDim.x, 0.0));
     if (threadIdx.x == 0) {
         *L.dsum_out = total;
         st->fix_count = 0u;
