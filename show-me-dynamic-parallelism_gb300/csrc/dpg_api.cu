@@ -55,6 +55,17 @@ void dev_free(dpg_ctx* c, void* p) {
     else cudaFree(p);
 }
 
+// A few pinned host words for flags the host reads back without a stream synchronisation.
+dpg_status host_words(dpg_ctx* c, unsigned** out) {
+    if (!c->host_words) {
+        void* p = nullptr;
+        DPG_CUDA_TRY(cudaHostAlloc(&p, 64, cudaHostAllocDefault));
+        c->host_words = static_cast<unsigned*>(p);
+    }
+    *out = c->host_words;
+    return DPG_OK;
+}
+
 void* arena(dpg_ctx* c, Slot s, size_t bytes, dpg_status* status) {
     Buf& b = c->bufs[s];
     if (bytes == 0) bytes = 16;
@@ -675,7 +686,25 @@ dpg_status run_pagerank(dpg_ctx* c, dpg_graph* g, const int32_t* d_outdeg, const
     L.dsum_out = dsum;
     float* init_rank_dst = conv ? rk[0] : (o.iterations == 0 ? d_rank : nullptr);
     DPG_CUDA_TRY(launch_pagerank_init(L, init_rank, init_rank_dst, c->st, c->stream, c->sm_count, &c->prof));
+    // With a tolerance the convergence test is pipelined one sweep deep: sweep it+1 is queued before
+    // the host reads sweep it's flag (pinned memory, an event), so the device does not idle on the
+    // read. A sweep queued after the converged one writes only buffers of the other parity (ranks,
+    // contributions, dangling sum, flag), so the converged ranks stay where the count says.
+    unsigned* hflags = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    if (conv) {
+        DPG_TRY(host_words(c, &hflags));
+        for (cudaEvent_t& e : ev) DPG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    struct Events {
+        cudaEvent_t* e;
+        ~Events() {
+            if (e[0]) cudaEventDestroy(e[0]);
+            if (e[1]) cudaEventDestroy(e[1]);
+        }
+    } ev_guard{ev};
     int64_t sweeps = 0;
+    int32_t pending = -1;  // sweep whose flag is on its way to the host
     for (int32_t it = 0; it < o.iterations; ++it) {
         L.x = contrib[it & 1];
         L.y = contrib[(it + 1) & 1];
@@ -684,8 +713,8 @@ dpg_status run_pagerank(dpg_ctx* c, dpg_graph* g, const int32_t* d_outdeg, const
         if (conv) {
             L.rank_prev = rk[it & 1];
             L.rank_out = rk[(it + 1) & 1];
-            L.nonstop = nonstop;
-            DPG_CUDA_TRY(cudaMemsetAsync(nonstop, 0, sizeof(unsigned), c->stream));
+            L.nonstop = nonstop + (it & 1);
+            DPG_CUDA_TRY(cudaMemsetAsync(L.nonstop, 0, sizeof(unsigned), c->stream));
         } else {
             L.rank_prev = nullptr;
             L.nonstop = nullptr;
@@ -694,10 +723,17 @@ dpg_status run_pagerank(dpg_ctx* c, dpg_graph* g, const int32_t* d_outdeg, const
         DPG_CUDA_TRY(launch_pagerank_sweep(L, c->st, c->stream, c->sm_count, &c->prof));
         ++sweeps;
         if (conv) {
-            unsigned h = 0;
-            DPG_CUDA_TRY(cudaMemcpyAsync(&h, nonstop, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-            DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-            if (h == 0) break;
+            DPG_CUDA_TRY(cudaMemcpyAsync(hflags + 2 + (it & 1), L.nonstop, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                         c->stream));
+            DPG_CUDA_TRY(cudaEventRecord(ev[it & 1], c->stream));
+            if (pending >= 0) {
+                DPG_CUDA_TRY(cudaEventSynchronize(ev[pending & 1]));
+                if (hflags[2 + (pending & 1)] == 0) {
+                    --sweeps;  // the sweep just queued is surplus
+                    break;
+                }
+            }
+            pending = it;
         }
     }
     if (conv) {
@@ -943,7 +979,7 @@ dpg_status run_pagerank_grad(dpg_ctx* c, dpg_graph* g, const float* d_w, const f
                      static_cast<float*>(arena(c, S_PRG_V3, nv * 4, &st))};
     double* part = static_cast<double*>(arena(c, S_PRG_PART, static_cast<size_t>(nb) * 8, &st));
     double* red = static_cast<double*>(arena(c, S_PRG_RED, 2 * 8, &st));
-    unsigned* flags = static_cast<unsigned*>(arena(c, S_PRG_FLAGS, 16, &st));  // [0] ticket, [1] nonstop
+    unsigned* flags = static_cast<unsigned*>(arena(c, S_PRG_FLAGS, 16, &st));  // [0] ticket, [1..2] nonstop
     if (st != DPG_OK) return st;
     DPG_CUDA_TRY(cudaMemsetAsync(flags, 0, 16, c->stream));
     // Out-weight sums W = A 1 and the weights in transposed-slot order.
@@ -958,10 +994,28 @@ dpg_status run_pagerank_grad(dpg_ctx* c, dpg_graph* g, const float* d_w, const f
     L.part = part;
     L.ticket = flags;
     L.damping = static_cast<float>(o.damping);
+    // The convergence test is pipelined one sweep deep: sweep it+1 is queued before the host reads
+    // sweep it's flag (copied to pinned memory, waited on with an event), so the device does not
+    // idle on the read. When sweep it converged, sweep it+1 is surplus: it wrote only the other
+    // vector, y, the reduction slot and flag of its own parity and (forward) the contributions,
+    // none of which is read afterwards, so stepping the vector swap back restores sweep it's result.
+    unsigned* hflags = nullptr;
+    DPG_TRY(host_words(c, &hflags));
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    for (cudaEvent_t& e : ev) DPG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    struct Events {
+        cudaEvent_t* e;
+        ~Events() {
+            cudaEventDestroy(e[0]);
+            cudaEventDestroy(e[1]);
+        }
+    } ev_guard{ev};
     auto sweeps_until = [&](int mode, int32_t cap, double eps, float** cur, float** nxt, dpg_graph* sg,
                             const float* vals, const float* x_of_cur, int64_t* done) -> dpg_status {
         // Every loop starts from the reduction its init pass left in red[0].
+        int32_t pending = -1;  // sweep whose flag is on its way to the host
         for (int32_t it = 0; it < cap; ++it) {
+            unsigned* dflag = flags + 1 + (it & 1);
             DPG_TRY(run_spmv(c, sg, vals, x_of_cur ? x_of_cur : *cur, y));
             L.mode = mode;
             L.y = y;
@@ -970,18 +1024,27 @@ dpg_status run_pagerank_grad(dpg_ctx* c, dpg_graph* g, const float* d_w, const f
             L.red_in = red + (it & 1);
             L.red_out = red + ((it + 1) & 1);
             L.epsilon = static_cast<float>(eps);
-            L.nonstop = eps > 0 ? flags + 1 : nullptr;
-            if (eps > 0) DPG_CUDA_TRY(cudaMemsetAsync(flags + 1, 0, 4, c->stream));
+            L.nonstop = eps > 0 ? dflag : nullptr;
+            if (eps > 0) DPG_CUDA_TRY(cudaMemsetAsync(dflag, 0, 4, c->stream));
             DPG_CUDA_TRY(launch_pr_vec(L, c->sm_count, c->stream, &c->prof));
             std::swap(*cur, *nxt);
             ++*done;
             if (eps > 0) {
-                unsigned h = 0;
-                DPG_CUDA_TRY(cudaMemcpyAsync(&h, flags + 1, 4, cudaMemcpyDeviceToHost, c->stream));
-                DPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-                if (h == 0) break;
+                DPG_CUDA_TRY(cudaMemcpyAsync(hflags + (it & 1), dflag, 4, cudaMemcpyDeviceToHost, c->stream));
+                DPG_CUDA_TRY(cudaEventRecord(ev[it & 1], c->stream));
+                if (pending >= 0) {
+                    DPG_CUDA_TRY(cudaEventSynchronize(ev[pending & 1]));
+                    if (hflags[pending & 1] == 0) {
+                        std::swap(*cur, *nxt);
+                        --*done;
+                        pending = -1;
+                        break;
+                    }
+                }
+                pending = it;
             }
         }
+        if (pending >= 0) DPG_CUDA_TRY(cudaEventSynchronize(ev[pending & 1]));
         return DPG_OK;
     };
 
@@ -1099,6 +1162,7 @@ dpg_status dpg_ctx_destroy(dpg_ctx* c) {
     for (auto& b : c->bufs) cudaFree(b.p);
     cudaFree(c->st);
     cudaFree(c->trace);
+    if (c->host_words) cudaFreeHost(c->host_words);
     // Blocks still held by orphaned graphs keep the pool alive until they are freed.
     if (c->pool) cudaMemPoolDestroy(c->pool);
     if (c->aux_stream) {

@@ -136,6 +136,7 @@ struct dpg_ctx {
     cudaMemPool_t pool = nullptr;
     // Second stream, created on first use: work that overlaps an upload on `stream` (event-ordered).
     cudaStream_t aux_stream = nullptr;
+    unsigned* host_words = nullptr;  // pinned, 16 words (host_words())
 };
 
 struct dpg_graph {
@@ -187,6 +188,7 @@ cudaError_t dev_alloc(dpg_ctx* c, T** p, size_t bytes) {
 }
 void dev_free(dpg_ctx* c, void* p);
 void* arena(dpg_ctx* c, Slot s, size_t bytes, dpg_status* status);
+dpg_status host_words(dpg_ctx* c, unsigned** out);
 dpg_status check_device(dpg_ctx* c);
 dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* offsets, const int32_t* col,
                                const int32_t* weights, bool device_ptrs, dpg_graph** out);
