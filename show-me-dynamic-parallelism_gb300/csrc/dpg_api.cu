@@ -545,7 +545,10 @@ void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const d
         o->solution = DPG_SOL_DIROPT;  // BFS: direction-optimizing; SSSP runs it as DPG_SOL_BINNED
     }
     if (o->threshold <= 0) o->threshold = DPG_REF_THRESHOLD;
-    if (o->hub_threshold <= 0) o->hub_threshold = 32;
+    // Degree from which a frontier vertex is cut into grid-wide chunks. Measured on R-MAT 24 (4
+    // sources): SSSP 9.06 ms at 32, 8.14 at 64, 7.81 at 128, 8.08 at 256; BFS (direction-optimizing)
+    // 1.84 / 1.76 / 1.77 / 1.77 ms. At R-MAT 22, SSSP takes 2.59 / 2.28 / 2.35 / 2.36 ms.
+    if (o->hub_threshold <= 0) o->hub_threshold = 128;
     if (o->solution == DPG_SOL_GRID) o->hub_threshold = o->threshold;
     if (o->max_iterations <= 0) {
         const int64_t cap = static_cast<int64_t>(g->V) + 2;
