@@ -58,18 +58,6 @@ __device__ __forceinline__ int pad(int i) { return i + (i >> 5); }
 
 enum { kModeSpmv = 0, kModePagerank = 1 };
 
-// x[c], from the shared-memory cache when c is one of the `hot` most gathered (renamed) columns.
-__device__ __forceinline__ float gather_x(const RowGatherLaunch& L, const float* s_hot, int c) {
-    return c < L.hot ? s_hot[c] : __ldg(L.x + c);
-}
-
-template <int MODE>
-__device__ __forceinline__ float load_product(const RowGatherLaunch& L, const float* s_hot, int e) {
-    const int c = __ldg(L.col + e);
-    if (MODE == kModeSpmv) return __ldg(L.vals + e) * gather_x(L, s_hot, c);
-    return gather_x(L, s_hot, c);
-}
-
 // PageRank epilogue of one row: new rank, next contribution, dangling mass, convergence flag.
 // od / pos are the row's out-degree and contribution slot (perm[v] with renamed columns).
 __device__ __forceinline__ void pr_epilogue(const RowGatherLaunch& L, int v, float sum, float base, int od, int pos,
@@ -237,21 +225,35 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
             Tn[k] = t < ntiles ? __ldg(L.plan.tiles + t) : make_int4(0, 0, 0, 0);
             infon[k] = t < ntiles ? __ldg(L.plan.lane_info + t * 32 + lane) : 0;
         }
-        // Phase 2: the gathers of every tile.
+        // Phase 2: the gathers of every tile. Both forms keep the hot test a select between a shared
+        // and a global load (written as an if/else it became a divergent branch: PageRank 0.192 ms
+        // per sweep against 0.176 ms). PageRank keeps its gathers under the (almost always warp-
+        // uniform) `j < nnz` test. SpMV issues them with no branch at all, the shared-memory read
+        // unconditional (entry 0 for cold columns; the launch allocates at least one) and the
+        // value load predicated, so the gather and its value load go out together: 204 -> 255 GTEPS
+        // on R-MAT 22. The unconditional shared read costs PageRank 1.4 %, hence the two forms.
 #pragma unroll
         for (int k = 0; k < KT; ++k) {
             const int nb = T[k].z, nnz = T[k].w;
 #pragma unroll
             for (int i = 0; i < kIpl; ++i) {
                 const int j = i * 32 + lane;
-                float v = 0.0f;
-                if (j < nnz) {
-                    v = gather_x(L, s_hot, cols[k][i]);
-                    if (MODE == kModeSpmv) v *= __ldg(L.vals + nb + j);
+                const int c = cols[k][i];
+                if constexpr (MODE == kModeSpmv) {
+                    const bool hot = c < L.hot;
+                    const float hv = s_hot[hot ? c : 0];
+                    float gv = 0.0f;
+                    if (!hot) gv = __ldg(L.x + c);
+                    const float a = j < nnz ? __ldg(L.vals + nb + j) : 0.0f;
+                    pv[k][i] = j < nnz ? (hot ? hv : gv) * a : 0.0f;
+                } else {
+                    float v = 0.0f;
+                    if (j < nnz) v = c < L.hot ? s_hot[c] : __ldg(L.x + c);
+                    pv[k][i] = v;
                 }
-                pv[k][i] = v;
             }
         }
+
         // Phase 3: each tile through the staging area.
 #pragma unroll
         for (int k = 0; k < KT; ++k) {
@@ -664,7 +666,8 @@ cudaError_t launch_row_sweep(const RowGatherLaunch& L, DevStatus* st, cudaStream
     constexpr int KT = MODE == kModeSpmv ? DPG_GATHER_TILES_SPMV : DPG_GATHER_TILES_PR;
     int gb, fb, bt;
     rowgather_grid(sm_count, &gb, &fb, &bt);
-    const size_t smem = rowgather_staging_bytes() + sizeof(float) * static_cast<size_t>(L.hot);
+    // At least one hot entry: the SpMV gather reads entry 0 for cold columns.
+    const size_t smem = rowgather_staging_bytes() + sizeof(float) * static_cast<size_t>(L.hot > 0 ? L.hot : 1);
     cudaError_t err = prepare_rowgather<MODE>(smem);
     if (err != cudaSuccess) return err;
     {
