@@ -206,17 +206,22 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
                 const int j = i * 32 + lane;
                 cols[k][i] = j < nnz ? __ldg(L.col + nb + j) : 0;
             }
+            // Predicated loads rather than branches, so they go out with the column loads.
             od0[k] = 0;
             pos0[k] = 0;
             od1[k] = 0;
             pos1[k] = 0;
-            if (MODE == kModePagerank && lane < nrows) {
-                od0[k] = __ldg(L.outdeg + row + lane);
-                pos0[k] = L.perm ? __ldg(L.perm + row + lane) : row + lane;
-            }
-            if (MODE == kModePagerank && lane + 32 < nrows) {
-                od1[k] = __ldg(L.outdeg + row + lane + 32);
-                pos1[k] = L.perm ? __ldg(L.perm + row + lane + 32) : row + lane + 32;
+            if (MODE == kModePagerank) {
+                const bool in0 = lane < nrows, in1 = lane + 32 < nrows;
+                od0[k] = in0 ? __ldg(L.outdeg + row + lane) : 0;
+                od1[k] = in1 ? __ldg(L.outdeg + row + lane + 32) : 0;
+                if (L.perm) {
+                    pos0[k] = in0 ? __ldg(L.perm + row + lane) : 0;
+                    pos1[k] = in1 ? __ldg(L.perm + row + lane + 32) : 0;
+                } else {
+                    pos0[k] = row + lane;
+                    pos1[k] = row + lane + 32;
+                }
             }
         }
 #pragma unroll
@@ -261,19 +266,18 @@ __global__ void __launch_bounds__(kBlock) rowgather_kernel(RowGatherLaunch L) {
             const int row = T[k].x, nrows = T[k].y, nb = T[k].z, nnz = T[k].w;
             if (nrows < 0) {
                 // Hub segment: fixed-order lane sums, then a butterfly; partial goes to the fix-up.
+                // Values past the segment's end are 0 (phase 2), so every lane adds all of its own.
                 float acc = 0.0f;
 #pragma unroll
-                for (int i = 0; i < kIpl; ++i)
-                    if (i * 32 + lane < nnz) acc += pv[k][i];
+                for (int i = 0; i < kIpl; ++i) acc += pv[k][i];
                 acc = warp_sum_f32(acc);
                 if (lane == 0) L.partial[-(nrows + 1)] = acc;
                 continue;
             }
+            // All 8 values are staged (0 past nnz; pad(255) = 262 is inside the 264-entry row), so the
+            // stores need no predicate; the walk reads only the first nnz of them as nonzeros.
 #pragma unroll
-            for (int i = 0; i < kIpl; ++i) {
-                const int j = i * 32 + lane;
-                if (j < nnz) val[pad(j)] = pv[k][i];
-            }
+            for (int i = 0; i < kIpl; ++i) val[pad(i * 32 + lane)] = pv[k][i];
             __syncwarp();
             // Merge-path: lane owns merge items [d0, d1) starting at row r0; the plan's mask says
             // which of them are row ends (emit the open row) and which are nonzeros (take one).
