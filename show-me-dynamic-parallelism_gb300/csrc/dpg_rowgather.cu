@@ -68,9 +68,15 @@ __device__ __forceinline__ void pr_epilogue(const RowGatherLaunch& L, int v, flo
     if (L.rank_prev && fabsf(nv - __ldg(L.rank_prev + v)) > L.epsilon) *L.nonstop = 1u;
     // Only vertices with out-arcs are ever gathered (they are the columns), so the contribution
     // slot of a dangling vertex is free: a batch parks its rank there for the per-graph reduction.
-    if (od > 0) L.y[pos] = nv / static_cast<float>(od);
-    else if (L.vgraph) L.y[pos] = nv;
-    else dang += static_cast<double>(nv);
+    // The division runs for every row (by 1 for a dangling one) so a warp's rows do not diverge
+    // around it; only the stores and the dangling sum depend on the out-degree.
+    const float q = nv / static_cast<float>(od > 0 ? od : 1);
+    if (L.vgraph) {
+        L.y[pos] = od > 0 ? q : nv;
+    } else {
+        if (od > 0) L.y[pos] = q;
+        if (od <= 0) dang += static_cast<double>(nv);
+    }
 }
 
 __device__ __forceinline__ void pr_epilogue(const RowGatherLaunch& L, int v, float sum, float base, double& dang) {
