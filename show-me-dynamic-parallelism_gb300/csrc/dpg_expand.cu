@@ -385,16 +385,13 @@ __device__ __forceinline__ void relax_batch(const ExpandParams& P, const PushCtx
             ok[u] = bits != 0u && tag_or(Q.dirty + v[u], Q.tag, bits);
         }
     } else {
+        // Inactive lanes load arc 0 (the adjacency always holds at least one entry) and the label of
+        // its head, so the loads need no branch; only the atomic depends on act.
         int cand[U], cur[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            v[u] = 0;
-            row[u] = 0;
-            cand[u] = 0;
-            if (act[u]) Op::load_edge(P, e[u], du[u], v[u], row[u], cand[u]);
-        }
+        for (int u = 0; u < U; ++u) Op::load_edge(P, act[u] ? e[u] : 0, du[u], v[u], row[u], cand[u]);
 #pragma unroll
-        for (int u = 0; u < U; ++u) cur[u] = (Op::kPeek && act[u]) ? __ldcg(P.label + v[u]) : 0;
+        for (int u = 0; u < U; ++u) cur[u] = Op::kPeek ? __ldcg(P.label + v[u]) : 0;
 #pragma unroll
         for (int u = 0; u < U; ++u)
             ok[u] = act[u] && Op::want(v[u], cand[u], cur[u]) && Op::commit(P, v[u], cand[u]);
