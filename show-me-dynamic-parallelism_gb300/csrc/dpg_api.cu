@@ -840,7 +840,8 @@ dpg_status graph_create_common(dpg_ctx* c, int32_t V, int64_t E, const int32_t* 
 // Everything between the upload and the sweeps runs on the device, on the aux stream, overlapped
 // with the upload of the columns; the host only issues work and waits once:
 //   - the offsets and out-degrees upload first. Then the offsets are validated on the device and
-//     the row plan is built on the device from them;
+//     the row plan (tiles, hub lists, each lane's start row and row-end mask) is built on the device
+//     from them, into capacity-sized buffers the graph keeps;
 //   - in an in-edge CSR a vertex's column count is its out-degree, so the frequency order of the
 //     column renaming comes from the out-degrees. The order is only a renaming and every row keeps
 //     its nonzero order, so the sums are the same with any order; out-degrees that disagree with
@@ -862,11 +863,14 @@ dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in
     const size_t nv = static_cast<size_t>(V), ne = static_cast<size_t>(E);
     int32_t* scratch = nullptr;
     PlanBuild pb;
+    uint16_t* lane_info = nullptr;  // capacity-sized; the graph keeps it
     cudaEvent_t ev_in = nullptr, ev_done = nullptr, ev_chunk[kRelabelChunks] = {};
     auto release = [&]() {
         if (c->aux_stream) cudaStreamSynchronize(c->aux_stream);
         dev_free(c, scratch);
         scratch = nullptr;
+        dev_free(c, lane_info);
+        lane_info = nullptr;
         plan_build_free(c, &pb);
         for (cudaEvent_t& ev : ev_chunk) {
             if (ev) cudaEventDestroy(ev);
@@ -895,7 +899,8 @@ dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in
         (e = dev_alloc(c, &g->perm, nv * 4)) != cudaSuccess || (e = dev_alloc(c, &g->inv, nv * 4)) != cudaSuccess ||
         (e = dev_alloc(c, &g->pcol, ne * 4)) != cudaSuccess ||
         (e = dev_alloc(c, &scratch, frequency_order_scratch_bytes(V))) != cudaSuccess ||
-        (e = plan_build_alloc(c, V, E, &pb)) != cudaSuccess)
+        (e = plan_build_alloc(c, V, E, &pb)) != cudaSuccess ||
+        (e = dev_alloc(c, &lane_info, 32 * sizeof(uint16_t) * static_cast<size_t>(pb.caps.tiles))) != cudaSuccess)
         return fail(set_error(DPG_ERR_CAPACITY, std::string("graph allocation: ") + cudaGetErrorString(e)));
     if ((e = cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming)) != cudaSuccess)
@@ -923,6 +928,9 @@ dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = plan_build_launch(pb, g->off, V, E, info, s1);
+    if (e == cudaSuccess)
+        e = launch_tile_lane_starts_dev(pb.tiles, &info->totals[0], pb.caps.tiles, &info->bad, g->off, lane_info, s1,
+                                        c->sm_count);
     if (e == cudaSuccess) e = launch_frequency_order(d_outdeg, V, scratch, g->perm, g->inv, s1);
     for (int k = 0; k < kRelabelChunks && e == cudaSuccess; ++k) {
         const int64_t b = std::min<int64_t>(E, k * step), n = std::min<int64_t>(E, b + step) - b;
@@ -941,8 +949,22 @@ dpg_status graph_create_pull(dpg_ctx* c, int32_t V, int64_t E, const int32_t* in
         return fail(vs != DPG_OK ? vs : set_error(DPG_ERR_INVALID_ARG, "offsets are not a valid CSR"));
     }
     if (h.bad & 1) return fail(set_error(DPG_ERR_INVALID_ARG, "column index out of range"));
-    const dpg_status ps = plan_finish(g, &pb, h);
-    if (ps != DPG_OK) return fail(ps);
+    // The graph adopts the capacity-sized plan buffers as they are (it lives for one call).
+    const int64_t nt = h.totals[0], nsm = h.totals[1], nbg = h.totals[2], nsg = h.totals[3];
+    if (nt < 0 || nt > pb.caps.tiles || nsm < 0 || nsm > pb.caps.hubs || nbg < 0 || nbg > pb.caps.hubs || nsg < 0 ||
+        nsg > INT32_MAX)
+        return fail(set_error(DPG_ERR_CAPACITY, "row plan exceeds its capacity"));
+    g->plan.ntiles = static_cast<int32_t>(nt);
+    g->plan.nhub_small = static_cast<int32_t>(nsm);
+    g->plan.nhub_big = static_cast<int32_t>(nbg);
+    g->plan.nseg = static_cast<int32_t>(nsg);
+    g->plan.tiles = pb.tiles;
+    g->plan.hubs_small = pb.hubs_small;
+    g->plan.hubs_big = pb.hubs_big;
+    g->plan.lane_info = lane_info;
+    pb.tiles = pb.hubs_small = pb.hubs_big = nullptr;
+    lane_info = nullptr;
+    g->plan_ready = true;
     release();
     g->relabel_ready = true;
     c->graphs.insert(g);

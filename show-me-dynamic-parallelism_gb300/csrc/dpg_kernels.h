@@ -286,6 +286,10 @@ cudaError_t launch_frequency_order(const int32_t* counts, int32_t V, int32_t* sc
 
 // Fills plan.lane_info from the tiles and the offsets (once per graph).
 cudaError_t launch_tile_lane_starts(const RowPlanDev& plan, const int32_t* off, cudaStream_t s, int sm_count);
+// The same over a plan whose tile count is on the device (*d_ntiles, at most cap), skipped when
+// *bad has bit 4 (offsets failed their check).
+cudaError_t launch_tile_lane_starts_dev(const int4* tiles, const int64_t* d_ntiles, int64_t cap, const int* bad,
+                                        const int32_t* off, uint16_t* lane_info, cudaStream_t s, int sm_count);
 
 // Grid shape used by the row-gather kernels (needed to size dpart/dfix).
 void rowgather_grid(int sm_count, int* gather_blocks, int* fix_blocks, int* block_threads);

@@ -402,11 +402,19 @@ __global__ void __launch_bounds__(kInitBlock) pr_init_kernel(RowGatherLaunch L, 
 // (row end r-1) + r <= 8 * lane (the row ends the lane's first merge item comes after), and which
 // of the lane's 8 merge items are row ends rather than nonzeros. With both, the gather kernel walks
 // its items without reading any row end.
-__global__ void tile_lane_starts_kernel(const int4* __restrict__ tiles, int ntiles, const int32_t* __restrict__ off,
+// With d_ntiles the tile count is read on the device (clamped to cap), and a set bad-offsets flag
+// makes the kernel do nothing: the plan it would read was built from offsets that failed the check.
+__global__ void tile_lane_starts_kernel(const int4* __restrict__ tiles, int ntiles, const int64_t* d_ntiles,
+                                        int64_t cap, const int* bad, const int32_t* __restrict__ off,
                                         uint16_t* __restrict__ lane_info) {
     const int lane = threadIdx.x & 31;
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
+    if (d_ntiles) {
+        if (bad && (*reinterpret_cast<const volatile int*>(bad) & 4)) return;
+        const int64_t n = *d_ntiles;
+        ntiles = static_cast<int>(n < cap ? n : cap);
+    }
     for (int t = w; t < ntiles; t += nw) {
         const int4 T = __ldg(tiles + t);
         int lo = 0;
@@ -444,7 +452,14 @@ __global__ void tile_lane_starts_kernel(const int4* __restrict__ tiles, int ntil
 
 cudaError_t launch_tile_lane_starts(const RowPlanDev& plan, const int32_t* off, cudaStream_t s, int sm_count) {
     if (plan.ntiles > 0)
-        tile_lane_starts_kernel<<<sm_count * 8, 256, 0, s>>>(plan.tiles, plan.ntiles, off, plan.lane_info);
+        tile_lane_starts_kernel<<<sm_count * 8, 256, 0, s>>>(plan.tiles, plan.ntiles, nullptr, 0, nullptr, off,
+                                                             plan.lane_info);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile_lane_starts_dev(const int4* tiles, const int64_t* d_ntiles, int64_t cap, const int* bad,
+                                        const int32_t* off, uint16_t* lane_info, cudaStream_t s, int sm_count) {
+    tile_lane_starts_kernel<<<sm_count * 8, 256, 0, s>>>(tiles, 0, d_ntiles, cap, bad, off, lane_info);
     return cudaGetLastError();
 }
 
