@@ -205,11 +205,58 @@ struct PushCtx {
     unsigned* far_count;
     int* far_min;
     int threshold;
+    // The warp's push buffer in shared memory (see flush_pushes) and its share of the frontier
+    // statistics, added to mf / nf once per iteration.
+    int* buf_v;
+    int2* buf_se;
+    unsigned* buf_n;
+    unsigned long long* buf_mf;
+    unsigned* buf_nf;
 };
+
+// Frontier vertices a warp collects in shared memory before it reserves their queue slots with one
+// atomic: every warp appending to the same global counter serialised on that address (R-MAT 24:
+// about 3 M appends per SSSP solve, 0.5 M in one bottom-up BFS step).
+constexpr int kPushBuf = 256;
+constexpr unsigned long long kPushBufferWork = 65536;  // arcs per iteration from which pushes are buffered
 
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) {
     return *reinterpret_cast<const volatile unsigned*>(p);
 }
+// The warp's buffered frontier vertices go to the global queue behind one reservation, and its
+// frontier statistics to mf / nf. All 32 lanes call it; every warp calls it before the iteration's
+// grid barrier, so the next iteration sees the whole frontier.
+__device__ __forceinline__ void flush_pushes(const ExpandParams& P, const PushCtx& Q) {
+    if (!Q.buf_n) return;  // this iteration pushes straight to the queue
+    const int lane = lane_id();
+    const unsigned n = *reinterpret_cast<volatile unsigned*>(Q.buf_n);
+    if (n) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(Q.qcount, n);
+        base = __shfl_sync(kFullMask, base, 0);
+        for (unsigned i = lane; i < n; i += 32) {
+            const unsigned pos = base + i;
+            if (pos < static_cast<unsigned long long>(P.ws.cap_v)) {
+                __stcg(Q.qv + pos, Q.buf_v[i]);
+                __stcg(Q.qse + pos, Q.buf_se[i]);
+            } else {
+                raise_error(P.st, DPG_ERR_CAPACITY, 11);
+            }
+        }
+    }
+    __syncwarp();
+    if (lane == 0) {
+        *Q.buf_n = 0u;
+        if (Q.mf && *Q.buf_nf) {
+            atomicAdd(Q.mf, *Q.buf_mf);
+            atomicAdd(Q.nf, *Q.buf_nf);
+            *Q.buf_mf = 0ull;
+            *Q.buf_nf = 0u;
+        }
+    }
+    __syncwarp();
+}
+
 // Called by all 32 lanes together with U candidate slots each; ok[u] marks slots whose relaxation
 // improved vertex v[u]. Vertices below the chunking degree go to the small queue with one
 // warp-aggregated append for all U slots; chunked vertices get their chunk range from one
@@ -254,15 +301,22 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
         degs += ok[u] ? static_cast<unsigned long long>(e[u] - s[u]) : 0ull;
         pushed += ok[u] ? 1u : 0u;
     }
-    if (Q.mf) {  // frontier statistics for the direction choice
+    if (Q.mf) {  // frontier statistics for the direction choice (added up per warp when buffering)
         degs = warp_sum_u64(degs);
         pushed = static_cast<unsigned>(warp_sum_u64(pushed));
         if (lane == 0 && pushed) {
-            atomicAdd(Q.mf, degs);
-            atomicAdd(Q.nf, pushed);
+            if (Q.buf_n) {
+                *Q.buf_mf += degs;
+                *Q.buf_nf += pushed;
+            } else {
+                atomicAdd(Q.mf, degs);
+                atomicAdd(Q.nf, pushed);
+            }
         }
     }
-    if (cnt) {
+    if (cnt > static_cast<unsigned>(kPushBuf) || !Q.buf_n) {
+        // A batch larger than the buffer (512-arc chunks), or a caller without one: its own
+        // reservation.
         unsigned base = 0;
         if (lane == 0) base = atomicAdd(Q.qcount, cnt);
         base = __shfl_sync(kFullMask, base, 0);
@@ -279,6 +333,25 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
             }
             base += static_cast<unsigned>(__popc(m[u]));
         }
+    } else if (cnt) {
+        unsigned n0 = *reinterpret_cast<volatile unsigned*>(Q.buf_n);
+        if (n0 + cnt > static_cast<unsigned>(kPushBuf)) {
+            flush_pushes(P, Q);
+            n0 = 0;
+        }
+        unsigned base = n0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (ok[u] && !chunked[u]) {
+                const unsigned pos = base + static_cast<unsigned>(__popc(m[u] & lt));
+                Q.buf_v[pos] = v[u];
+                Q.buf_se[pos] = make_int2(s[u], e[u]);
+            }
+            base += static_cast<unsigned>(__popc(m[u]));
+        }
+        __syncwarp();
+        if (lane == 0) *Q.buf_n = n0 + cnt;
+        __syncwarp();
     }
     if (kClassify) {
 #pragma unroll
@@ -516,6 +589,12 @@ __global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(Expa
     __shared__ int c_wsum[kWarps];
     __shared__ int c_n;
     __shared__ int c_total;
+    // Per-warp frontier push buffers (flush_pushes).
+    __shared__ int p_v[kWarps][kPushBuf];
+    __shared__ int2 p_se[kWarps][kPushBuf];
+    __shared__ unsigned p_n[kWarps];
+    __shared__ unsigned long long p_mf[kWarps];
+    __shared__ unsigned p_nf[kWarps];
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -523,6 +602,11 @@ __global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(Expa
     const unsigned nwarps = gridDim.x * kWarps;
     unsigned long long my_edges = 0, my_pops = 0;
     if (threadIdx.x == 0) c_n = 0;
+    if (lane == 0) {
+        p_n[warp] = 0u;
+        p_mf[warp] = 0ull;
+        p_nf[warp] = 0u;
+    }
     __syncthreads();
 
     // Direction-optimizing BFS (Beamer, Asanovic, Patterson, "Direction-Optimizing Breadth-First
@@ -589,6 +673,13 @@ __global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(Expa
                 P.trace[4 * j + 3] = bottom_up ? 2ull : 0ull;
             }
         }
+        // Push buffering pays only when an iteration's pushes are many (the global counter is then
+        // contended); with the few pushes of a high-diameter graph's iterations its flush is one more
+        // round trip per iteration. The arcs to relax (vertices plus 256-arc chunks) decide, the
+        // same for every CTA. On R-MAT 24 it cut SSSP from 7.6 to 5.6 ms and BFS from 1.70 to 1.16
+        // ms; on the 4096^2 grid, buffering every iteration cost near-far SSSP 11 %.
+        const unsigned long long work = static_cast<unsigned long long>(n) + 256ull * nch + (split ? far_n : 0u);
+        const bool buffered = work >= kPushBufferWork || (kDirOpt && bottom_up);
         // Parity selects are written as ternaries so the pointer pairs stay in registers.
         const PushCtx Q = {p ? P.ws.qv[0] : P.ws.qv[1], p ? P.ws.qse[0] : P.ws.qse[1],
                            P.ws.qcount + (j + 1) % 3, p ? P.ws.bmp[0] : P.ws.bmp[1],
@@ -597,7 +688,9 @@ __global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(Expa
                            kDirOpt ? P.mf + (j + 1) % 3 : nullptr, kDirOpt ? P.nf + (j + 1) % 3 : nullptr,
                            kNearFar ? P.far[split ? (pile + 1) % 3 : pile] : nullptr,
                            kNearFar ? P.far_count + (split ? (pile + 1) % 3 : pile) : nullptr,
-                           kNearFar ? P.far_min + (split ? (pile + 1) % 3 : pile) : nullptr, threshold};
+                           kNearFar ? P.far_min + (split ? (pile + 1) % 3 : pile) : nullptr, threshold,
+                           buffered ? p_v[warp] : nullptr, buffered ? p_se[warp] : nullptr,
+                           buffered ? &p_n[warp] : nullptr, &p_mf[warp], &p_nf[warp]};
         const int32_t* qv_cur = p ? P.ws.qv[1] : P.ws.qv[0];
         const int2* qse_cur = p ? P.ws.qse[1] : P.ws.qse[0];
         uint32_t* bmp_cur = p ? P.ws.bmp[1] : P.ws.bmp[0];
@@ -774,6 +867,7 @@ __global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(Expa
                 }
             }
         }
+        flush_pushes(P, Q);
         if (!grid_barrier(P.st, gridDim.x, P.timeout_ns)) break;
         if (kNearFar && split) pile = (pile + 1) % 3;
     }
