@@ -717,24 +717,49 @@ __global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(Expa
             }
         } else if (kDirOpt && bottom_up) {
             // Bottom-up: every unvisited vertex looks for an in-neighbour on the frontier's level j.
-            for (int64_t base = static_cast<int64_t>(gwarp) * 32; base < P.V; base += static_cast<int64_t>(nwarps) * 32) {
-                const int v = static_cast<int>(base) + lane;
-                bool found = false;
-                if (v < P.V && __ldcg(P.label + v) == DPG_UNDEFINED_LEVEL) {
-                    const int b = __ldg(P.t_off + v), e = __ldg(P.t_off + v + 1);
-                    int k = b;
-                    for (; k < e; ++k)
-                        if (__ldcg(P.label + __ldg(P.t_col + k)) == j) {
-                            found = true;
-                            break;
-                        }
-                    my_edges += static_cast<unsigned long long>((found ? k + 1 : e) - b);
-                    if (found) {
-                        P.label[v] = j + 1;
+            // A lane takes kBu vertices at a time and issues their loads together (level, in-arc
+            // range, first in-arc and its level), so the common cases (a parent at the first in-arc,
+            // no in-arcs) cost one chain of round trips for all of them; the others go on arc by arc.
+            // The parent test and the arcs counted are those of a one-vertex-at-a-time scan.
+            constexpr int kBu = 4;
+            const int64_t stride = static_cast<int64_t>(nwarps) * 32 * kBu;
+            for (int64_t base = static_cast<int64_t>(gwarp) * 32 * kBu; base < P.V; base += stride) {
+                int vv[kBu], b[kBu], e[kBu], t0[kBu];
+                bool unv[kBu], found[kBu];
+#pragma unroll
+                for (int r = 0; r < kBu; ++r) {
+                    const int64_t x = base + 32 * r + lane;
+                    vv[r] = x < P.V ? static_cast<int>(x) : 0;
+                    unv[r] = x < P.V && __ldcg(P.label + vv[r]) == DPG_UNDEFINED_LEVEL;
+                }
+#pragma unroll
+                for (int r = 0; r < kBu; ++r) {
+                    b[r] = unv[r] ? __ldg(P.t_off + vv[r]) : 0;
+                    e[r] = unv[r] ? __ldg(P.t_off + vv[r] + 1) : 0;
+                }
+#pragma unroll
+                for (int r = 0; r < kBu; ++r) t0[r] = b[r] < e[r] ? __ldg(P.t_col + b[r]) : -1;
+#pragma unroll
+                for (int r = 0; r < kBu; ++r) found[r] = t0[r] >= 0 && __ldcg(P.label + t0[r]) == j;
+#pragma unroll
+                for (int r = 0; r < kBu; ++r) {
+                    if (!unv[r]) continue;
+                    int k = b[r];
+                    if (!found[r]) {
+                        for (k = b[r] + 1; k < e[r]; ++k)
+                            if (__ldcg(P.label + __ldg(P.t_col + k)) == j) {
+                                found[r] = true;
+                                break;
+                            }
+                    }
+                    my_edges += static_cast<unsigned long long>((found[r] ? k + 1 : e[r]) - b[r]);
+                    if (found[r]) {
+                        P.label[vv[r]] = j + 1;
                         my_pops += 1;
                     }
                 }
-                push_converged<Op, kClassify, CH>(P, Q, found, found ? v : 0);
+#pragma unroll
+                for (int r = 0; r < kBu; ++r) push_converged<Op, kClassify, CH>(P, Q, found[r], found[r] ? vv[r] : 0);
             }
         } else if (POL == DPG_SOL_BLOCK) {
             const unsigned per_round = gridDim.x * kWarps;
