@@ -250,7 +250,10 @@ typedef struct dpg_cdp_stats {
 dpg_status dpg_bfs_cdp_dev(dpg_ctx* ctx, const dpg_graph* g, int32_t source, int32_t variant, int32_t pending_limit,
                            int32_t* d_level, dpg_cdp_stats* stats);
 
-/* ---- one-shot host calls: the whole reference wrapper in one call (upload, solve, download) ---- */
+/* ---- one-shot host calls: the whole reference wrapper in one call (upload, solve, download) ----
+ * dpg_pagerank_f32_host validates the offsets and columns, plans the row gathers and renames the
+ * columns on the device while the columns upload; errors are those of dpg_graph_create, and the
+ * ranks are bitwise those of dpg_graph_create + dpg_pagerank_f32 on the same arrays. */
 dpg_status dpg_sssp_host(dpg_ctx* ctx, int32_t V, int64_t E, const int32_t* offsets,
                          const int32_t* col, const int32_t* weights, int32_t source,
                          const dpg_expand_opts* opts, int32_t* h_dist);
