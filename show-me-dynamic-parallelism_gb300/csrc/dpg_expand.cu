@@ -263,7 +263,7 @@ __device__ __forceinline__ void flush_pushes(const ExpandParams& P, const PushCt
 // warp-aggregated atomic per slot and the warp writes every chunk descriptor.
 template <class Op, bool kClassify, int CH, int U>
 __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx& Q, bool (&ok)[U],
-                                           const int (&v)[U], const int (&row)[U]) {
+                                           const int (&v)[U], const int (&row)[U], const int2* se_pre = nullptr) {
     bool any = false;
 #pragma unroll
     for (int u = 0; u < U; ++u) any |= ok[u];
@@ -275,12 +275,16 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
 #pragma unroll
         for (int u = 0; u < U; ++u) ok[u] = ok[u] && (old[u] & (1u << (v[u] & 31))) == 0u;
     }
+    // Row ranges: loaded here, or passed in by a caller that fetched them ahead (se_pre[u]).
     int s[U], e[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         s[u] = 0;
         e[u] = 0;
-        if (ok[u]) {
+        if (se_pre) {
+            s[u] = ok[u] ? se_pre[u].x : 0;
+            e[u] = ok[u] ? se_pre[u].y : 0;
+        } else if (ok[u]) {
             s[u] = __ldg(P.off + row[u]);
             e[u] = __ldg(P.off + row[u] + 1);
         }
@@ -483,10 +487,11 @@ __device__ __forceinline__ void relax_batch(const ExpandParams& P, const PushCtx
 
 // Push of vertices whose label index is their row (single-source operators).
 template <class Op, bool kClassify, int CH>
-__device__ __forceinline__ void push_converged(const ExpandParams& P, const PushCtx& Q, bool ok, int v) {
+__device__ __forceinline__ void push_converged(const ExpandParams& P, const PushCtx& Q, bool ok, int v,
+                                               const int2* se_pre = nullptr) {
     bool okb[1] = {ok};
     const int vb[1] = {v};
-    push_batch<Op, kClassify, CH, 1>(P, Q, okb, vb, vb);
+    push_batch<Op, kClassify, CH, 1>(P, Q, okb, vb, vb, se_pre);
 }
 
 // Relaxation of one candidate per lane (all lanes call it together).
@@ -718,8 +723,9 @@ __global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(Expa
         } else if (kDirOpt && bottom_up) {
             // Bottom-up: every unvisited vertex looks for an in-neighbour on the frontier's level j.
             // A lane takes kBu vertices at a time and issues their loads together (level, in-arc
-            // range, first in-arc and its level), so the common cases (a parent at the first in-arc,
-            // no in-arcs) cost one chain of round trips for all of them; the others go on arc by arc.
+            // range, first in-arc and its level; the out-row range a push needs comes with the in-row
+            // range), so the common cases (a parent at the first in-arc, no in-arcs) cost one chain of
+            // round trips for all of them; the others go on arc by arc.
             // The parent test and the arcs counted are those of a one-vertex-at-a-time scan.
             constexpr int kBu = 4;
             const int64_t stride = static_cast<int64_t>(nwarps) * 32 * kBu;
@@ -732,10 +738,12 @@ __global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(Expa
                     vv[r] = x < P.V ? static_cast<int>(x) : 0;
                     unv[r] = x < P.V && __ldcg(P.label + vv[r]) == DPG_UNDEFINED_LEVEL;
                 }
+                int2 ose[kBu];  // out-row ranges for the push, fetched with the in-row ranges
 #pragma unroll
                 for (int r = 0; r < kBu; ++r) {
                     b[r] = unv[r] ? __ldg(P.t_off + vv[r]) : 0;
                     e[r] = unv[r] ? __ldg(P.t_off + vv[r] + 1) : 0;
+                    ose[r] = unv[r] ? make_int2(__ldg(P.off + vv[r]), __ldg(P.off + vv[r] + 1)) : make_int2(0, 0);
                 }
 #pragma unroll
                 for (int r = 0; r < kBu; ++r) t0[r] = b[r] < e[r] ? __ldg(P.t_col + b[r]) : -1;
@@ -759,7 +767,8 @@ __global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(Expa
                     }
                 }
 #pragma unroll
-                for (int r = 0; r < kBu; ++r) push_converged<Op, kClassify, CH>(P, Q, found[r], found[r] ? vv[r] : 0);
+                for (int r = 0; r < kBu; ++r)
+                    push_converged<Op, kClassify, CH>(P, Q, found[r], found[r] ? vv[r] : 0, &ose[r]);
             }
         } else if (POL == DPG_SOL_BLOCK) {
             const unsigned per_round = gridDim.x * kWarps;
