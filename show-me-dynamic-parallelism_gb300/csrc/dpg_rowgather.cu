@@ -5,10 +5,12 @@
 // serialises a thread; the consolidation variants hand rows of degree >= 64 to CDP children that
 // block-reduce them (SpMV_kernel.cu:196-216, pagerank_kernel.cu:357-382).
 //
-// Here the rows are cut on the host into warp tiles of at most 256 merge items (rows + nonzeros):
-//   - a normal tile holds whole rows of degree <= 255; one warp stages the tile's row ends and
-//     gathered products in shared memory, each lane walks 8 consecutive merge items (merge-path
-//     over row ends and nonzeros), and a warp segmented scan joins rows that cross lanes;
+// Here the rows are cut (on the device, once per graph) into warp tiles of at most 256 merge items
+// (rows + nonzeros):
+//   - a normal tile holds whole rows of degree <= 255; one warp stages the tile's gathered
+//     products in shared memory, each lane walks 8 consecutive merge items (merge-path over row
+//     ends and nonzeros, from a start row and a row-end mask the plan keeps per lane), and a warp
+//     segmented scan joins rows that cross lanes;
 //   - a row of degree > 255 (a hub) is split into 256-nonzero segments whose partial sums are
 //     combined afterwards, in segment order, by the hub fix-up kernel.
 // Every sum has a fixed order, so results are bit-reproducible run to run; no float atomics.
@@ -29,7 +31,8 @@ namespace dpg {
 namespace {
 
 // One CTA per SM: its dynamic shared memory holds the hot-value cache (the first `hot` renamed
-// entries of x, i.e. the most gathered columns) and its warps' tile staging.
+// entries of x, i.e. the most gathered columns) and its warps' tile staging. DPG_GATHER_BLOCK (and
+// the tile counts below) are build-time tuning knobs (DPG_NVCC_EXTRA); the defaults are measured.
 #ifndef DPG_GATHER_BLOCK
 #define DPG_GATHER_BLOCK 1024
 #endif
