@@ -77,7 +77,7 @@ typedef struct dpg_expand_opts {
     int32_t hub_threshold;   /* BINNED: degree at which a vertex is expanded grid-wide; 0 -> auto */
     int32_t max_iterations;  /* 0 -> V + 2 (label-correcting never needs more) */
     double timeout_seconds;  /* limit of each grid-barrier wait; 0 -> 10 s */
-    int32_t delta;           /* NEARFAR: threshold step; 0 -> twice the mean arc weight */
+    int32_t delta;           /* NEARFAR: threshold step; 0 -> 32 x the mean arc weight */
 } dpg_expand_opts;
 
 typedef struct dpg_pr_opts {

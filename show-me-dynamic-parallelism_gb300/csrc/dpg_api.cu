@@ -536,7 +536,10 @@ dpg_status run_color(dpg_ctx* c, dpg_graph* g, const dpg_expand_opts* in_opts, i
 }
 
 // Near-far threshold step in units of the mean arc weight (see dpg_expand.cu, DPG_SOL_NEARFAR).
-constexpr double kNearFarStep = 2.0;
+// Measured (2 sources): on the 4096^2 grid (weights 1..1000) SSSP takes 120 ms at 2x the mean
+// weight, 80 at 8x, 67 at 32x, 65 at 64x and 73 at 256x; on R-MAT 22 and 24 (weights 1..255) 32x
+// is within 5 % of the binned expansion, and 2x is 15-50 % slower.
+constexpr double kNearFarStep = 32.0;
 
 void fill_expand_defaults(const dpg_expand_opts* in, dpg_expand_opts* o, const dpg_graph* g) {
     if (in) *o = *in;
