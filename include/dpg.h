@@ -63,7 +63,8 @@ typedef enum dpg_solution {
     DPG_SOL_GRID = 4,   /* degree >= threshold: consolidated grid-wide, expanded by every CTA */
     DPG_SOL_BINNED = 5, /* warp scan-gather below hub_threshold, grid-wide edge chunks above */
     DPG_SOL_DIROPT = 6, /* BFS: binned top-down steps, bottom-up steps over in-arcs while the frontier
-                           is large (direction-optimizing); SSSP runs DPG_SOL_BINNED */
+                           is large (direction-optimizing); SSSP runs DPG_SOL_NEARFAR on graphs without
+                           vertices of degree >= hub_threshold and E <= 8V, else DPG_SOL_BINNED */
     DPG_SOL_NEARFAR = 7 /* SSSP: binned steps over the vertices below a distance threshold, the rest
                            deferred to a far pile (near-far); BFS runs DPG_SOL_DIROPT */
 } dpg_solution;
