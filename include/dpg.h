@@ -127,6 +127,11 @@ dpg_status dpg_graph_destroy(dpg_graph* g);
  * counterpart in the reference. */
 dpg_status dpg_graph_relabel(dpg_graph* g, int32_t enable);
 dpg_status dpg_graph_info(const dpg_graph* g, int32_t* V, int64_t* E, int32_t* weighted);
+/* Row-gather plan of the graph (built on first use, on the device): warp tiles (normal tiles plus
+ * hub segments), hub rows fixed up per thread (<= 8 segments) and per warp, and hub segments.
+ * No counterpart in the reference. */
+dpg_status dpg_graph_plan_info(dpg_graph* g, int32_t* tiles, int32_t* hubs_small, int32_t* hubs_big,
+                               int32_t* segments);
 
 /* ---- SSSP (replaces SSSP_GPU, apps/sssp/src/sssp_wrapper.cu:304-341) --------------------------- */
 /* dist[v] = shortest distance from source, DPG_INF_COST when unreachable. Weights must be >= 0. */

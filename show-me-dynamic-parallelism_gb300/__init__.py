@@ -142,6 +142,7 @@ _SIGS = {
     "dpg_graph_destroy": [_P],
     "dpg_graph_relabel": [_P, c_int32],
     "dpg_graph_info": [_P, POINTER(c_int32), POINTER(c_int64), POINTER(c_int32)],
+    "dpg_graph_plan_info": [_P, POINTER(c_int32), POINTER(c_int32), POINTER(c_int32), POINTER(c_int32)],
     "dpg_sssp": [_P, _P, c_int32, POINTER(ExpandOpts), _P],
     "dpg_sssp_dev": [_P, _P, c_int32, POINTER(ExpandOpts), _P],
     "dpg_bfs": [_P, _P, c_int32, POINTER(ExpandOpts), _P],
@@ -472,6 +473,12 @@ class Graph:
         _check(lib().dpg_graph_create_device(ctx.handle, V, E, c_void_p(d_offsets), c_void_p(d_col),
                                              c_void_p(d_weights) if d_weights else None, byref(h)))
         return cls(ctx, None, None, _handle=h, _V=V, _E=E)
+
+    def plan_info(self) -> dict:
+        """Row-gather plan counts: tiles (normal tiles and hub segments), small and big hubs, segments."""
+        t, hs, hb, sg = c_int32(), c_int32(), c_int32(), c_int32()
+        _check(lib().dpg_graph_plan_info(self.handle, byref(t), byref(hs), byref(hb), byref(sg)))
+        return {"tiles": t.value, "hubs_small": hs.value, "hubs_big": hb.value, "segments": sg.value}
 
     def set_relabel(self, enable: bool) -> None:
         """Column renaming by frequency for SpMV/PageRank (on by default; results are identical)."""

@@ -1324,6 +1324,18 @@ dpg_status dpg_graph_info(const dpg_graph* g, int32_t* V, int64_t* E, int32_t* w
     return DPG_OK;
 }
 
+dpg_status dpg_graph_plan_info(dpg_graph* g, int32_t* tiles, int32_t* hubs_small, int32_t* hubs_big,
+                               int32_t* segments) {
+    if (!g || !g->ctx) return set_error(DPG_ERR_INVALID_ARG, "null graph or destroyed context");
+    DPG_TRY(use_device(g->ctx));
+    if (g->V > 0) DPG_TRY(ensure_plan(g));
+    if (tiles) *tiles = g->plan.ntiles;
+    if (hubs_small) *hubs_small = g->plan.nhub_small;
+    if (hubs_big) *hubs_big = g->plan.nhub_big;
+    if (segments) *segments = g->plan.nseg;
+    return DPG_OK;
+}
+
 dpg_status dpg_sssp_dev(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_expand_opts* opts, int32_t* d_dist) {
     DPG_TRY(use_device(c));
     return run_expand(c, g, source, opts, d_dist, false);

@@ -8,18 +8,11 @@ LPT loads stay within the list-scheduling bound."""
 from __future__ import annotations
 
 import os
-import socket
 
 import numpy as np
 import pytest
 
 NSRC, SWEEPS, NGRAPHS, SEED = 2, 5, 24, 77
-
-
-def _free_port() -> int:
-    with socket.socket() as s:
-        s.bind(("127.0.0.1", 0))
-        return s.getsockname()[1]
 
 
 def _solve(dpg, oracle, spec, k):
@@ -32,7 +25,7 @@ def _solve(dpg, oracle, spec, k):
     return k, np.stack(dist), r
 
 
-def _rank_main(rank, world, port, out_path):
+def _rank_main(rank, world, store_path, out_path):
     import sys
 
     import torch.distributed as dist
@@ -42,8 +35,8 @@ def _rank_main(rank, world, port, out_path):
     from conftest import dpg
     import oracle
 
-    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
-    dist.init_process_group("gloo", rank=rank, world_size=world)
+    # A file rendezvous in the test's temporary directory: no port to race for.
+    dist.init_process_group("gloo", init_method=f"file://{store_path}", rank=rank, world_size=world)
     specs = dpg.rmat_batch_specs(NGRAPHS, seed=SEED, vmin=64, vmax=4096)
     cost = np.array([v * ef * (NSRC + SWEEPS) for v, ef in specs], np.int64)
     owner, load = dpg.partition_lpt(cost, world)
@@ -86,7 +79,8 @@ def test_two_rank_sharded_batch_matches_one_process(tmp_path):
 
     world = 2
     out = str(tmp_path / "gathered.pkl")
-    mp.start_processes(_rank_main, args=(world, _free_port(), out), nprocs=world, start_method="spawn", join=True)
+    store = str(tmp_path / "rendezvous")
+    mp.start_processes(_rank_main, args=(world, store, out), nprocs=world, start_method="spawn", join=True)
     with open(out, "rb") as f:
         gathered = pickle.load(f)
     owners = [np.array(o) for _, o, _, _ in gathered]

@@ -159,6 +159,46 @@ def test_one_shot_pagerank_host_call(ctx, orc, graphs):
     assert np.max(np.abs(r - r64) / r64) <= TOL
 
 
+def _plan_counts(off, rows_per_range=2048, tile_items=256, hub_degree=255, small_segs=8):
+    """The row plan's greedy tiling, restated: per range of rows, consecutive rows share a tile while
+    their merge items (rows + nonzeros) fit in 256; a row above degree 255 is cut into 256-nonzero
+    segments (a hub, fixed up per thread with <= 8 segments, else per warp)."""
+    off = np.asarray(off, np.int64)
+    V = len(off) - 1
+    tiles = small = big = segs = 0
+    for r0 in range(0, V, rows_per_range):
+        cur_rows = cur_items = 0
+        for r in range(r0, min(V, r0 + rows_per_range)):
+            d = int(off[r + 1] - off[r])
+            if d > hub_degree:
+                if cur_rows:
+                    tiles += 1
+                cur_rows = cur_items = 0
+                n = (d + tile_items - 1) // tile_items
+                tiles += n
+                segs += n
+                small, big = (small + 1, big) if n <= small_segs else (small, big + 1)
+                continue
+            if cur_items + d + 1 > tile_items:
+                tiles += 1
+                cur_rows = cur_items = 0
+            cur_rows += 1
+            cur_items += d + 1
+        if cur_rows:
+            tiles += 1
+    return {"tiles": tiles, "hubs_small": small, "hubs_big": big, "segments": segs}
+
+
+@pytest.mark.parametrize("name", ["data_test", "rmat12", "rmat16", "hubs", "grid"])
+def test_device_row_plan_matches_restated_greedy(ctx, graphs, name):
+    # The plan is built on the device (count, scan and write passes); its counts must equal the
+    # greedy tiling restated here, for the out-edge CSR (SpMV) and the in-edge CSR (PageRank).
+    g = graphs[name]
+    in_off, in_col, _ = _pr_inputs(g)
+    for off, col in ((g.offsets, g.col), (in_off, in_col)):
+        assert dpg.Graph(ctx, off, col).plan_info() == _plan_counts(off)
+
+
 @pytest.mark.parametrize("name", ["rmat12", "hubs", "data_test"])
 def test_one_shot_matches_graph_path_bitwise(ctx, graphs, name):
     # The one-shot call renames columns by the out-degree array while the columns upload; the graph
