@@ -268,19 +268,24 @@ dpg_status dpg_pagerank_f32_host(dpg_ctx* ctx, int32_t V, int64_t E, const int32
                                  const dpg_pr_opts* opts, float* h_rank);
 
 /* ---- SSSP without allocation (no counterpart in the reference) -------------------------------- */
-/* For callers that cannot allocate device memory or let a library do it: code running inside a
- * CUDA-graph capture, and engines that own the whole device pool and forbid cudaMalloc/cudaFree
- * behind their back. Runs the binned SSSP kernel on caller-owned device inputs and output, with
- * its workspace in a fixed 7 MiB __device__ array inside libdpg.so (held by every GPU that loads the
- * library until exit). Limits: V <= 262144 and E <= 4194304, else DPG_ERR_CAPACITY.
- *   d_offsets[V+1]      CSR offsets
- *   d_adj_pairs[2*E]    interleaved (neighbour, weight) int32 pairs, 8-byte aligned, weights in [0, 2^30)
+/* For callers that must not allocate device memory, nor let a library do it: a serving engine
+ * that reserves the whole device pool at start-up for its own arena (cudaMalloc would find nothing
+ * left, and cudaMalloc/cudaFree can synchronise the device under its other streams), or a plugin
+ * host that gives its plugins only buffers it owns. Runs the binned SSSP kernel on caller-owned
+ * device inputs and output, with its workspace in a fixed 7 MiB __device__ array inside libdpg.so
+ * (held by every GPU that loads the library until exit). Limits: V <= 262144 and E <= 4194304,
+ * else DPG_ERR_CAPACITY.
+ *   d_offsets[V+1]      CSR offsets, rising from 0 to E
+ *   d_adj_pairs[2*E]    interleaved (neighbour, weight) int32 pairs, 8-byte aligned, neighbours in
+ *                       [0, V), weights in [0, 2^30)
  *   d_dist[V]           output distances (DPG_INF_COST when unreachable)
  *   stream              cudaStream_t (NULL = legacy default stream); the call synchronises it
- * Every call shares the array and clears what must start at zero; calls whose GPU work overlaps
- * (two threads or streams) race on it. The first call on a device looks up the array's address
- * (cudaGetSymbolAddress); make that first call before any stream capture. Calls no cudaMalloc,
- * cudaFree or other allocating routine. */
+ * The graph is checked on the device before anything is relaxed: a violation of the ranges above
+ * returns DPG_ERR_INVALID_ARG. Every call shares the array and clears what must start at zero;
+ * calls whose GPU work overlaps (two threads or streams) race on it. The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress) and keeps it: make that first call before
+ * any stream capture, and reload the library after a cudaDeviceReset of that device. Calls no
+ * cudaMalloc, cudaFree or other allocating routine. */
 dpg_status dpg_sssp_noalloc_dev(int32_t V, int64_t E, const int32_t* d_offsets, const int32_t* d_adj_pairs,
                                 int32_t source, int32_t* d_dist, void* stream);
 

@@ -1,13 +1,14 @@
 // SSSP entry point that allocates nothing: dpg_sssp_noalloc_dev (declared in include/dpg.h).
 //
-// Why it exists: some callers of this library cannot allocate device memory themselves or let a
-// library do it. Examples are code running inside a CUDA-graph capture, and engines that own the
-// whole device pool (a serving runtime with a fixed arena, an allocator-less plugin host) and
-// forbid cudaMalloc/cudaFree behind their back. The regular entry points need a dpg_ctx and a
-// dpg_graph, and both allocate (status block, stream, frontier arena, device CSR). This one runs
-// the same persistent SSSP kernel (binned work mapping) on caller-owned inputs and outputs, with
-// its frontier queues, bitmaps, chunk lists and status word carved out of one file-scope
-// __device__ array.
+// Why it exists: some callers of this library must not allocate device memory, nor let a library
+// do it for them. A serving engine that reserves the whole device pool at start-up and hands out
+// slices of its own arena has nothing left for cudaMalloc, and its other streams would stall on
+// the device-wide synchronisation that cudaMalloc/cudaFree can imply. A plugin host that gives its
+// plugins only the buffers it owns, and audits every allocation, forbids them outright. The
+// regular entry points need a dpg_ctx and a dpg_graph, and both allocate (status block, stream,
+// frontier arena, device CSR). This one runs the same persistent SSSP kernel (binned work mapping)
+// on caller-owned inputs and outputs, with its frontier queues, bitmaps, chunk lists and status
+// words carved out of one file-scope __device__ array.
 //
 // Limits and sharing rules:
 //   * at most kNoAllocMaxVertices vertices and kNoAllocMaxArcs arcs; larger graphs are rejected
@@ -17,11 +18,18 @@
 //   * every call on a device uses the same array and leaves its contents behind; each call clears
 //     what must start at zero, but calls whose GPU work overlaps (two host threads, two streams)
 //     race on it, so callers must not let calls overlap;
+//   * the caller's CSR is checked on the device before the expansion runs (offsets rise from 0 to
+//     E, neighbour ids in [0, V), weights in [0, 2^30)); a bad graph returns DPG_ERR_INVALID_ARG
+//     and nothing is relaxed;
 //   * the first call on a device looks up the array's device address (cudaGetSymbolAddress, which
-//     may load the module); make that first call before any stream capture.
+//     may load the module) and keeps it for later calls on that device; make that first call
+//     before any stream capture. The kept address belongs to the device's primary context as it
+//     was at that call: after cudaDeviceReset the library must be reloaded before this entry
+//     point is used again on that device.
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -41,7 +49,7 @@ constexpr int kMaxDevices = 64;
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct NoAllocLayout {
-    size_t qv, qse, bmp, chunks, qcount, ccount, status, total;
+    size_t qv, qse, bmp, chunks, qcount, ccount, status, check, total;
 };
 
 constexpr NoAllocLayout layout_for(int64_t V, int64_t E) {
@@ -58,7 +66,8 @@ constexpr NoAllocLayout layout_for(int64_t V, int64_t E) {
     L.qcount = align256(sizeof(uint32_t) * 4);
     L.ccount = align256(sizeof(uint32_t) * 4);
     L.status = align256(sizeof(DevStatus));
-    L.total = 2 * (L.qv + L.qse + L.bmp + L.chunks) + L.qcount + L.ccount + L.status;
+    L.check = align256(sizeof(int));
+    L.total = 2 * (L.qv + L.qse + L.bmp + L.chunks) + L.qcount + L.ccount + L.status + L.check;
     return L;
 }
 
@@ -68,6 +77,26 @@ static_assert(layout_for(kNoAllocMaxVertices, kNoAllocMaxArcs).total <= kNoAlloc
 // The scratch itself. In host code this name is only a handle for cudaGetSymbolAddress; the kernels
 // receive the device address obtained below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// The caller's CSR, checked before anything is relaxed: *bad |= 1 for a neighbour id outside
+// [0, V), 2 for a weight outside [0, 2^30) (sums of two stay below 2^31), 4 for offsets that do
+// not rise from 0 to E. The reads stay inside the arrays the caller declared: offsets [0, V],
+// pairs [0, E).
+__global__ void noalloc_check_kernel(const int32_t* __restrict__ off, const int2* __restrict__ adj, int32_t V,
+                                     int64_t E, int* bad) {
+    const int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    int flags = 0;
+    for (int64_t v = tid; v < V; v += stride)
+        if (off[v + 1] < off[v]) flags |= 4;
+    if (tid == 0 && (off[0] != 0 || static_cast<int64_t>(off[V]) != E)) flags |= 4;
+    for (int64_t e = tid; e < E; e += stride) {
+        const int2 a = adj[e];
+        if (a.x < 0 || a.x >= V) flags |= 1;
+        if (a.y < 0 || a.y >= DPG_INF_COST) flags |= 2;
+    }
+    if (flags) atomicOr(bad, flags);
+}
 
 std::mutex g_scratch_mu;
 void* g_scratch_addr[kMaxDevices] = {};
@@ -128,13 +157,29 @@ extern "C" dpg_status dpg_sssp_noalloc_dev(int32_t V, int64_t E, const int32_t* 
     }
     ws.qcount = reinterpret_cast<uint32_t*>(p); p += Lo.qcount;
     ws.ccount = reinterpret_cast<uint32_t*>(p); p += Lo.ccount;
-    DevStatus* st = reinterpret_cast<DevStatus*>(p);
+    DevStatus* st = reinterpret_cast<DevStatus*>(p); p += Lo.status;
+    int* bad = reinterpret_cast<int*>(p);
 
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
-    // The status word keeps the previous call's contents: start this call from a clean one. The
-    // expansion's init kernel clears the queues' counters and both bitmaps.
+    // The status and check words keep the previous call's contents: start this call from clean
+    // ones. The expansion's init kernel clears the queues' counters and both bitmaps.
     e = cudaMemsetAsync(st, 0, sizeof(DevStatus), cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), cs);
     if (e != cudaSuccess) return set_error(DPG_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+    // The expansion trusts its graph (an out-of-range id would make it write outside d_dist), so the
+    // check completes before it is launched.
+    int check_blocks = static_cast<int>((std::max<int64_t>(V, E) + 255) / 256);
+    if (check_blocks > sm_count * 4) check_blocks = sm_count * 4;
+    noalloc_check_kernel<<<check_blocks, 256, 0, cs>>>(d_offsets, reinterpret_cast<const int2*>(d_adj_pairs), V, E,
+                                                       bad);
+    int flags = 0;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, bad, sizeof(int), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+    if (e != cudaSuccess) return set_error(DPG_ERR_CUDA, std::string("no-alloc graph check: ") + cudaGetErrorString(e));
+    if (flags & 4) return set_error(DPG_ERR_INVALID_ARG, "dpg_sssp_noalloc_dev: offsets must rise from 0 to E");
+    if (flags & 1) return set_error(DPG_ERR_INVALID_ARG, "dpg_sssp_noalloc_dev: neighbour id outside [0, V)");
+    if (flags & 2) return set_error(DPG_ERR_INVALID_ARG, "dpg_sssp_noalloc_dev: weight outside [0, 2^30)");
 
     ExpandLaunch L;
     L.off = d_offsets;
