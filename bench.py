@@ -55,6 +55,9 @@ def parse_args():
     ap.add_argument("--batch-graphs", type=int, default=512, help="graphs in --workload batch")
     ap.add_argument("--solution", type=int, default=-1, help="dpg.SOL_* id for --workload sssp/bfs (-1: default)")
     ap.add_argument("--no-relabel", action="store_true", help="turn off the column renaming of SpMV/PageRank")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) leg and the CPU baseline")
+    ap.add_argument("--ingest-traffic", metavar="CSV", help="write profiles/" + TRAFFIC_FILE + " from the ncu CSV "
+                    "of the traffic capture command, then exit")
     return ap.parse_args()
 
 
@@ -73,18 +76,83 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(name: str):
-    """DRAM bytes per launch recorded in profiles/<name> by an ncu capture (None when absent)."""
-    p = ROOT / "profiles" / name
+# The sources of the headline kernel (row gather + its plan) whose DRAM traffic an ncu capture records.
+GATHER_SOURCES = ["show-me-dynamic-parallelism_gb300/csrc/dpg_rowgather.cu",
+                  "show-me-dynamic-parallelism_gb300/csrc/dpg_layout.cu",
+                  "show-me-dynamic-parallelism_gb300/csrc/dpg_kernels.h",
+                  "show-me-dynamic-parallelism_gb300/build.py"]
+TRAFFIC_FILE = "traffic_rowgather_pagerank_rmat22.txt"
+TRAFFIC_KERNEL = "rowgather_kernel"
+# The command whose ncu output --ingest-traffic turns into profiles/<TRAFFIC_FILE> (one launch,
+# one pass: DRAM bytes only, on the headline workload after 40 gather launches of warm-up).
+TRAFFIC_COMMAND = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none "
+                   "-k regex:rowgather_kernel -s 40 -c 1 --csv --page raw --log-file gpurun_out/traffic.csv "
+                   "python bench.py --steps 3 --warmup 3 --no-extra --no-e2e")
+
+
+def sources_fingerprint(paths=GATHER_SOURCES) -> str:
+    import hashlib
+
+    h = hashlib.sha256()
+    for rel in paths:
+        h.update(rel.encode())
+        h.update((ROOT / rel).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def ingest_traffic(csv_path: str) -> int:
+    """Turns the raw-page CSV of TRAFFIC_COMMAND into profiles/<TRAFFIC_FILE>, stamped with the
+    fingerprint of the kernel sources it was captured from."""
+    import csv
+
+    rows = [r for r in csv.reader(open(csv_path)) if r]
+    hdr = next(i for i, r in enumerate(rows) if "Kernel Name" in r)
+    names = rows[hdr]
+    data = [r for r in rows[hdr + 1:] if len(r) == len(names) and TRAFFIC_KERNEL in r[names.index("Kernel Name")]]
+    if not data:
+        print(f"no {TRAFFIC_KERNEL} launch in {csv_path}", file=sys.stderr)
+        return 1
+    r = data[0]
+    val = {m: float(r[names.index(m)].replace(",", "")) for m in ("dram__bytes_read.sum", "dram__bytes_write.sum")}
+    units = rows[hdr + 1][names.index("dram__bytes_read.sum")] if len(rows) > hdr + 1 else ""
+    scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "KB": 1e3, "MB": 1e6, "GB": 1e9}.get(units.strip(), 1)
+    out = ROOT / "profiles" / TRAFFIC_FILE
+    out.write_text(
+        f"# DRAM bytes of one {TRAFFIC_KERNEL} launch (PageRank sweep, R-MAT scale 22), from ncu.\n"
+        f"# command: {TRAFFIC_COMMAND}\n"
+        f"# ingested by: python bench.py --ingest-traffic gpurun_out/traffic.csv\n"
+        f"sources_fingerprint = {sources_fingerprint()}\n"
+        f"kernel = {r[names.index('Kernel Name')]}\n"
+        f"dram__bytes_read.sum = {val['dram__bytes_read.sum'] * scale:.0f}\n"
+        f"dram__bytes_write.sum = {val['dram__bytes_write.sum'] * scale:.0f}\n")
+    print(out.read_text())
+    return 0
+
+
+def capture_traffic():
+    """(DRAM bytes per gather launch, note) from profiles/<TRAFFIC_FILE>; None when the file is
+    absent or was captured from other kernel sources than the ones built now."""
+    p = ROOT / "profiles" / TRAFFIC_FILE
     if not p.exists():
-        return None
+        return None, "no capture"
+    kv = {}
     for line in p.read_text().splitlines():
-        if line.strip().startswith("dram_bytes_per_full_launch"):
-            try:
-                return float(line.split("=")[1].split()[0])
-            except (IndexError, ValueError):
-                return None
-    return None
+        if "=" in line and not line.startswith("#"):
+            k, v = line.split("=", 1)
+            kv[k.strip()] = v.strip()
+    if kv.get("sources_fingerprint") != sources_fingerprint():
+        return None, "capture is of other kernel sources (stale)"
+    try:
+        return float(kv["dram__bytes_read.sum"]) + float(kv["dram__bytes_write.sum"]), "ncu capture of these sources"
+    except (KeyError, ValueError):
+        return None, "unreadable capture"
+
+
+def bench_config(world: int, V: int, E: int) -> dict:
+    """The workload's config, printed identically by both arms."""
+    return {"workload": WORKLOAD, "vertices": V, "arcs": E, "graph_seed": GRAPH_SEED,
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "l2": "inputs larger than L2 (in-arcs 268 MB > 129 MB), no flush"}
 
 
 def build_workload(dpg):
@@ -160,15 +228,21 @@ def cpu_pagerank_sample(orc, in_off, in_col, od, E, target_s=10.0):
 
 
 def run_reference(args, world, rank):
+    """The reference's PageRank on the host cores. The reference has no CPU PageRank (its only CPU
+    algorithm is bfs_cpu), so this times the oracle's restatement of pagerank_thread_pull_kernel and
+    its host loop (apps/pagerank/src/pagerank_kernel.cu:95-120, pagerank_wrapper.cu:147-241) on all
+    host threads. The graph is generated and transposed by the oracle as well: this arm loads no
+    library of the GPU implementation."""
     if rank != 0:
         return 0
-    import __graft_entry__
-
-    dpg = __graft_entry__.load_package()
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as orc
 
-    g, in_off, in_col, od = build_workload(dpg)
+    off, col, _ = orc.rmat_csr(SCALE, EDGE_FACTOR, GRAPH_SEED, weights=False)
+    in_off, in_col = orc.csr_transpose(off, col)
+    od = np.diff(off).astype(np.int32)
+    V, E = off.shape[0] - 1, col.shape[0]
+    del off, col
     threads = orc.num_threads()
     t0 = time.perf_counter()
     orc.pagerank_omp_f32(in_off, in_col, od, damping=DAMPING, total=1.0, iterations=1)
@@ -181,15 +255,14 @@ def run_reference(args, world, rank):
     for _ in range(steps):
         orc.pagerank_omp_f32(in_off, in_col, od, damping=DAMPING, total=1.0, iterations=sweeps)
     dt = time.perf_counter() - t0
-    value = g.E * sweeps * steps / dt / 1e9
+    value = E * sweeps * steps / dt / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "vertices": g.V, "arcs": g.E, "sweeps_per_step": sweeps,
-                   "note": "CPU restatement of pagerank_thread_pull_kernel + host loop; all host threads"},
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": bench_config(world, V, E),
         "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
-                         "sample": f"{steps} steps x {sweeps} sweeps on the full graph"},
+                         "sample": f"{steps} steps x {sweeps} sweeps of the pull PageRank restatement on the "
+                                   f"full scale-{SCALE} graph, all host threads (the reference has no CPU PageRank)"},
         "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -763,25 +836,29 @@ def run_dpg(args, world, rank, local):
     gather_avg_ms = ms_g / max(n_g, 1)
     bytes_sweep = 4 * (V + 1) + 4 * E + 12 * V  # in-offsets, in-arcs, contrib read, contrib write, outdeg read
     achieved = bytes_sweep / (gather_avg_ms / 1e3) / 1e9
-    traffic = profile_traffic("rowgather_pagerank_rmat22.md")
+    traffic, traffic_note = capture_traffic()
 
     # e2e: one-shot C-ABI call with pinned host buffers (upload, solve, download inside the region).
-    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
-    h_off, h_col, h_od = pin(in_off), pin(in_col), pin(od)
-    h_rank = torch.empty(V, dtype=torch.float32).pin_memory().numpy()
-    dpg.pagerank_host(ctx, h_off, h_col, h_od, out=h_rank, damping=DAMPING, iterations=SWEEPS)
-    e2e_steps = max(3, min(args.steps, 10))
-    if world > 1:
-        torch.distributed.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+        h_off, h_col, h_od = pin(in_off), pin(in_col), pin(od)
+        h_rank = torch.empty(V, dtype=torch.float32).pin_memory().numpy()
         dpg.pagerank_host(ctx, h_off, h_col, h_od, out=h_rank, damping=DAMPING, iterations=SWEEPS)
-    t_e2e = time.perf_counter() - t0
-    if world > 1:
-        tt = torch.tensor([t_e2e], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(tt.item())
-    e2e_value = E * SWEEPS * e2e_steps * world / t_e2e / 1e9
+        e2e_steps = max(3, min(args.steps, 10))
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            dpg.pagerank_host(ctx, h_off, h_col, h_od, out=h_rank, damping=DAMPING, iterations=SWEEPS)
+        t_e2e = time.perf_counter() - t0
+        if world > 1:
+            tt = torch.tensor([t_e2e], dtype=torch.float64, device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t_e2e = float(tt.item())
+        e2e = {"value": E * SWEEPS * e2e_steps * world / t_e2e / 1e9, "unit": "GTEPS", "steps": e2e_steps,
+               "h2d_bytes_per_step": int(h_off.nbytes + h_col.nbytes + h_od.nbytes),
+               "d2h_bytes_per_step": int(h_rank.nbytes)}
 
     if rank != 0:
         if world > 1:
@@ -792,25 +869,23 @@ def run_dpg(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "vertices": V, "arcs": E, "graph_seed": GRAPH_SEED,
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (in-arcs 268 MB > 129 MB), no flush"},
+        "config": bench_config(world, V, E),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "rowgather_kernel<PageRank>", "peak_source": peak_kind,
+                     "traffic": traffic, "traffic_source": traffic_note, "kernel": "rowgather_kernel<PageRank>",
+                     "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": bytes_sweep, "avg_launch_ms": gather_avg_ms},
-        "e2e": {"value": e2e_value, "unit": "GTEPS", "steps": e2e_steps,
-                "h2d_bytes_per_step": int(h_off.nbytes + h_col.nbytes + h_od.nbytes),
-                "d2h_bytes_per_step": int(h_rank.nbytes)},
+        "e2e": e2e,
         "gpu_launches": int(n_g + n_f + n_i),
         "kernel_ms": {"rowgather": ms_g, "fixup": ms_f, "init": ms_i},
     }
     if clocks:
         line["clocks"] = clocks
     if world == 1:
-        sys.path.insert(0, str(ROOT / "oracle"))
-        import oracle as orc
+        if not args.no_e2e:
+            sys.path.insert(0, str(ROOT / "oracle"))
+            import oracle as orc
 
-        line["cpu_baseline"] = cpu_pagerank_sample(orc, in_off, in_col, od, E)
+            line["cpu_baseline"] = cpu_pagerank_sample(orc, in_off, in_col, od, E)
         if not args.no_extra:
             del gi
             line["extra"] = extra_measurements(dpg, ctx, torch, g, peak, args.steps)
@@ -823,6 +898,8 @@ def run_dpg(args, world, rank, local):
 
 def main() -> int:
     args = parse_args()
+    if args.ingest_traffic:
+        return ingest_traffic(args.ingest_traffic)
     world, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, world, rank)

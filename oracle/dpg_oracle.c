@@ -301,12 +301,15 @@ int oracle_bfs_omp(int32_t V, const int32_t* off, const int32_t* col, int32_t sr
 }
 
 /* ------------------------------------------------------------------------------------ SpMV ---- */
-/* y[r] = sum_e data[e] * x[col[e]] in FP64 (csr_spmv_kernel); FLOAT_T is double in the reference. */
+/* y[r] = sum_e data[e] * x[col[e]] in FP64 (csr_spmv_kernel); FLOAT_T is double in the reference.
+ * `dot += data[i] * x[indices[i]]` is one fused multiply-add per nonzero as nvcc compiles it (its
+ * default contracts a*b+c), so the restatement uses fma() and matches the kernel's output bit for
+ * bit (checked against the reference kernel's own output in tests/golden/refgpu.npz). */
 void oracle_spmv_f64(int32_t V, const int32_t* off, const int32_t* col, const double* data, const double* x,
                      double* y) {
     for (int32_t r = 0; r < V; ++r) {
         double dot = 0.0;
-        for (int32_t e = off[r]; e < off[r + 1]; ++e) dot += data[e] * x[col[e]];
+        for (int32_t e = off[r]; e < off[r + 1]; ++e) dot = fma(data[e], x[col[e]], dot);
         y[r] = dot;
     }
 }
@@ -391,16 +394,22 @@ int64_t oracle_pagerank_f64(int32_t V, const int32_t* in_off, const int32_t* in_
     return sweeps;
 }
 
-/* The reference's FP32 arithmetic, in its order: per in-edge new += damping * (rank[p]/outdeg[p]),
- * then + rank_random_walk + rank_dangling_node (pagerank_kernel.cu:112-118), dangling summed in FP32
- * in dangling-vertex order (pagerank_wrapper.cu:214-221), stop when no |rank-new| > (float)epsilon. */
+/* The reference's FP32 arithmetic, in its order: per in-edge new = fma(damping, rank[p]/outdeg[p], new)
+ * (pagerank_kernel.cu:112-115; nvcc contracts `new_rank_tid += damping * rank` into one fused
+ * multiply-add), then + rank_random_walk + rank_dangling_node (:117). On the host:
+ * rank_random_walk = (1-damping)*TOTAL_RANK/V with float (1-damping) and the double TOTAL_RANK,
+ * rounded to float (pagerank_wrapper.cu:183); the dangling ranks summed in FP32 in vertex order and
+ * rank_dangling_node = damping * dangling / V in float (:210-221); continue while some
+ * |rank - new| (float) exceeds the double EPSILON (check_delta_kernel, pagerank_kernel.cu:72-81).
+ * epsilon < 0 runs exactly max_iterations sweeps. Matches the reference kernels' output bit for bit
+ * (tests/golden/refgpu.npz). */
 int64_t oracle_pagerank_ref_f32(int32_t V, const int32_t* in_off, const int32_t* in_col, const int32_t* outdeg,
-                                float damping, float total, int32_t init_zero, int32_t max_iterations,
-                                float epsilon, float* rank) {
+                                float damping, double total, int32_t init_zero, int32_t max_iterations,
+                                double epsilon, float* rank) {
     float* nr = (float*)malloc(sizeof(float) * (size_t)(V > 0 ? V : 1));
     if (!nr) return -1;
-    for (int32_t v = 0; v < V; ++v) rank[v] = init_zero ? 0.0f : total / (float)V;
-    const float rank_random_walk = (1 - damping) * total / (float)V;
+    for (int32_t v = 0; v < V; ++v) rank[v] = init_zero ? 0.0f : (float)total / (float)V;
+    const float rank_random_walk = (float)((double)(1.0f - damping) * total / (double)V);
     int64_t sweeps = 0;
     int nonstop = 1;
     while (nonstop && sweeps < max_iterations) {
@@ -408,19 +417,19 @@ int64_t oracle_pagerank_ref_f32(int32_t V, const int32_t* in_off, const int32_t*
         for (int32_t v = 0; v < V; ++v)
             if (outdeg[v] == 0) dangling_rank += rank[v];
         const float rank_dangling_node = damping * dangling_rank / (float)V;
-        nonstop = 0;
+        nonstop = epsilon < 0;
         for (int32_t v = 0; v < V; ++v) {
             float s = 0.0f;
             for (int32_t e = in_off[v]; e < in_off[v + 1]; ++e) {
                 int32_t p = in_col[e];
                 float r = rank[p] / (float)outdeg[p];
-                s += damping * r;
+                s = fmaf(damping, r, s);
             }
             s = s + rank_random_walk + rank_dangling_node;
             nr[v] = s;
         }
         for (int32_t v = 0; v < V; ++v) {
-            if (fabsf(rank[v] - nr[v]) > epsilon) nonstop = 1;
+            if ((double)fabsf(rank[v] - nr[v]) > epsilon) nonstop = 1;
             rank[v] = nr[v];
         }
         ++sweeps;
@@ -488,4 +497,125 @@ int64_t oracle_color(int32_t V, const int32_t* off, const int32_t* col, int32_t*
         ++rounds;
     }
     return rounds;
+}
+
+/* ------------------------------------------------------- synthetic graphs and CSR construction -- */
+/* These let the CPU arms of bench.py build the benchmark graph without the library under test.
+ *
+ * oracle_rmat_arcs restates the seeded counter-based R-MAT generator the benchmark uses (the
+ * library's dpg_rmat_arcs): arc e draws its 64-bit words from splitmix64(splitmix64(seed ^ e*K) +
+ * counter), four 16-bit quadrant draws per word, rejection of endpoints >= V, then a seeded
+ * bijection of the vertex ids; weight = wmin + draw(e, 2^32-1) % (wmax-wmin+1). The same seed thus
+ * gives the same arc list as the library, which the CPU-only tests check.
+ * oracle_csr_from_arcs restates convertCSR (common/global.cpp:192-235): a vertex's arcs appear in
+ * the reverse of their order in the input, as convertCSR pops each adjacency list from its back.
+ * oracle_csr_transpose restates invertGraph (common/global.cpp:237-277): in-row v lists the
+ * sources of v's in-arcs in descending source order (push_back over ascending sources, then
+ * popped from the back). */
+static uint64_t orc_mix(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+static uint64_t orc_draw(uint64_t seed, uint64_t stream, uint64_t counter) {
+    return orc_mix(orc_mix(seed ^ (stream * 0xD1B54A32D192ED03ull)) + counter);
+}
+
+static uint32_t orc_permute(uint32_t x, int bits, uint64_t seed) {
+    if (bits <= 0) return x;
+    const uint64_t mask = bits >= 32 ? 0xFFFFFFFFull : ((1ull << bits) - 1ull);
+    const int sh = bits / 2 + 1;
+    uint64_t y = x;
+    for (int round = 0; round < 3; ++round) {
+        const uint64_t k = orc_draw(seed, 0xA5A5ull + (uint64_t)round, 0);
+        y = (y ^ (k >> 40)) & mask;
+        y = (y * ((k & 0xFFFFFFFFull) | 1ull)) & mask;
+        if (sh < bits) y = (y ^ (y >> sh)) & mask;
+    }
+    return (uint32_t)y;
+}
+
+/* Returns 0, or -1 on bad arguments, or -2 when rejection sampling did not converge. */
+int oracle_rmat_arcs(int32_t scale, int32_t V, int64_t E, uint64_t seed, double a, double b, double c,
+                     int32_t wmin, int32_t wmax, int32_t permute, int32_t* src, int32_t* dst, int32_t* w) {
+    if (scale < 1 || scale > 30 || V < 1 || (int64_t)V > (1ll << scale) || E < 0) return -1;
+    const uint32_t ta = (uint32_t)llround(a * 65536.0);
+    const uint32_t tab = (uint32_t)llround((a + b) * 65536.0);
+    const uint32_t tabc = (uint32_t)llround((a + b + c) * 65536.0);
+    const uint64_t span = w ? (uint64_t)((int64_t)wmax - wmin + 1) : 1;
+    int failed = 0;
+#pragma omp parallel for schedule(static) reduction(| : failed)
+    for (int64_t e = 0; e < E; ++e) {
+        uint32_t u = 0, v = 0;
+        int ok = 0;
+        for (uint64_t attempt = 0; attempt <= 4097 && !ok; ++attempt) {
+            uint64_t word = 0;
+            u = v = 0;
+            for (int lvl = 0; lvl < scale; ++lvl) {
+                if (lvl % 4 == 0) word = orc_draw(seed, (uint64_t)e, attempt * 64 + (uint64_t)(lvl / 4));
+                const uint32_t r = (uint32_t)(word & 0xFFFFu);
+                word >>= 16;
+                u = 2 * u + (r >= tab);
+                v = 2 * v + ((r >= ta && r < tab) || r >= tabc);
+            }
+            if (permute) {
+                u = orc_permute(u, scale, seed);
+                v = orc_permute(v, scale, seed);
+            }
+            ok = (int64_t)u < V && (int64_t)v < V;
+        }
+        if (!ok) failed = 1;
+        src[e] = (int32_t)u;
+        dst[e] = (int32_t)v;
+        if (w) w[e] = wmin + (int32_t)(orc_draw(seed, (uint64_t)e, 0xFFFFFFFFull) % span);
+    }
+    return failed ? -2 : 0;
+}
+
+/* off[V+1], col[E] (and wout[E] when w and wout are given). Returns 0, or -1 on an id out of range. */
+int oracle_csr_from_arcs(int32_t V, int64_t E, const int32_t* src, const int32_t* dst, const int32_t* w,
+                         int32_t* off, int32_t* col, int32_t* wout) {
+    int64_t* fill = (int64_t*)calloc((size_t)V + 1, sizeof(int64_t));
+    if (!fill) return -2;
+    for (int64_t e = 0; e < E; ++e) {
+        if (src[e] < 0 || src[e] >= V || dst[e] < 0 || dst[e] >= V) {
+            free(fill);
+            return -1;
+        }
+        ++fill[src[e] + 1];
+    }
+    for (int32_t v = 0; v < V; ++v) fill[v + 1] += fill[v];
+    for (int32_t v = 0; v <= V; ++v) off[v] = (int32_t)fill[v];
+    /* Fill each row from its end, so the last arc of the input lands first. */
+    for (int32_t v = 0; v < V; ++v) fill[v] = off[v + 1];
+    for (int64_t e = 0; e < E; ++e) {
+        const int64_t p = --fill[src[e]];
+        col[p] = dst[e];
+        if (w && wout) wout[p] = w[e];
+    }
+    free(fill);
+    return 0;
+}
+
+int oracle_csr_transpose(int32_t V, const int32_t* off, const int32_t* col, int32_t* in_off, int32_t* in_col) {
+    const int64_t E = off[V];
+    int64_t* fill = (int64_t*)calloc((size_t)V + 1, sizeof(int64_t));
+    if (!fill) return -2;
+    for (int64_t e = 0; e < E; ++e) {
+        if (col[e] < 0 || col[e] >= V) {
+            free(fill);
+            return -1;
+        }
+        ++fill[col[e] + 1];
+    }
+    for (int32_t v = 0; v < V; ++v) fill[v + 1] += fill[v];
+    for (int32_t v = 0; v <= V; ++v) in_off[v] = (int32_t)fill[v];
+    for (int32_t v = 0; v < V; ++v) fill[v] = in_off[v + 1];
+    /* Ascending sources, each in-row filled from its end: the largest source ends up first. */
+    for (int32_t u = 0; u < V; ++u)
+        for (int32_t e = off[u]; e < off[u + 1]; ++e) in_col[--fill[col[e]]] = u;
+    free(fill);
+    return 0;
 }

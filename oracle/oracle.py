@@ -3,11 +3,14 @@
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs import this module, and only
 as the checker or as the timed CPU baseline. The product library (libdpg.so) never calls it.
 
-Two libraries:
-  * oracle/_build/liboracle.so — our C restatement of the reference algorithms (dpg_oracle.c);
+Libraries:
+  * oracle/_build/liboracle.so — our C restatement of the reference algorithms (dpg_oracle.c),
+    plus the benchmark graph generator and CSR/transpose builders the CPU arms use;
   * oracle/_ref/libref.so      — the reference's own host code (common/global.cpp loader + CSR +
     invertGraph, apps/bfs-rec/src/bfs_rec.cpp bfs_cpu), compiled from the reference tree by
-    oracle/Makefile when that tree is present. It does not exist where the reference is absent.
+    oracle/Makefile when that tree is present. It does not exist where the reference is absent;
+  * oracle/_ref/ref_*.cubin     — the reference's own kernels as device modules (ref_kernels.cu),
+    run by oracle/_build/librefgpu.so (ref_gpu_driver.cpp) only to generate tests/golden/refgpu.npz.
 """
 from __future__ import annotations
 
@@ -22,7 +25,20 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "_build" / "liboracle.so"
 REF_SO = HERE / "_ref" / "libref.so"
-REFERENCE_TREE = Path(os.environ.get("DPG_REFERENCE_TREE", "/root/reference"))
+
+
+def _find_reference_tree():
+    """The reference source tree: $DPG_REFERENCE_TREE, else a checkout named `reference` beside this
+    repository; None when neither holds the reference's common/global.cpp."""
+    cands = [Path(os.environ["DPG_REFERENCE_TREE"])] if os.environ.get("DPG_REFERENCE_TREE") else []
+    cands.append(HERE.parents[1] / "reference")
+    for c in cands:
+        if (c / "common" / "global.cpp").exists():
+            return c
+    return None
+
+
+REFERENCE_TREE = _find_reference_tree()
 
 INF = 1073741824
 UNDEFINED = 0x7FFFFFFF
@@ -40,9 +56,13 @@ _ORACLE_SIGS = {
     "oracle_spmv_omp_f32": ([c_int32, _P, _P, _P, _P, _P, c_int32], None),
     "oracle_pagerank_f64": ([c_int32, _P, _P, _P, c_double, c_double, c_int32, c_int32, c_double, _P, c_int32],
                             c_int64),
-    "oracle_pagerank_ref_f32": ([c_int32, _P, _P, _P, c_float, c_float, c_int32, c_int32, c_float, _P], c_int64),
+    "oracle_pagerank_ref_f32": ([c_int32, _P, _P, _P, c_float, c_double, c_int32, c_int32, c_double, _P], c_int64),
     "oracle_pagerank_omp_f32": ([c_int32, _P, _P, _P, c_float, c_float, c_int32, _P, c_int32], c_int64),
     "oracle_color": ([c_int32, _P, _P, _P], c_int64),
+    "oracle_rmat_arcs": ([c_int32, c_int32, c_int64, ctypes.c_uint64, c_double, c_double, c_double, c_int32, c_int32,
+                          c_int32, _P, _P, _P], c_int),
+    "oracle_csr_from_arcs": ([c_int32, c_int64, _P, _P, _P, _P, _P, _P], c_int),
+    "oracle_csr_transpose": ([c_int32, _P, _P, _P, _P], c_int),
 }
 _REF_SIGS = {
     "ref_load": ([c_char_p, c_int, POINTER(c_int), POINTER(c_longlong), POINTER(c_int)], c_int),
@@ -59,12 +79,15 @@ _ref = None
 
 
 def build(with_reference: bool | None = None) -> None:
-    """Compiles liboracle.so, and libref.so when the reference tree is present."""
+    """Compiles liboracle.so; where the reference tree is present, also libref.so (its host code) and
+    the device modules of its kernels (oracle/_ref/ref_*.cubin, for tests/golden/make_golden_gpu.py)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
     if with_reference is None:
-        with_reference = (REFERENCE_TREE / "common" / "global.cpp").exists()
+        with_reference = REFERENCE_TREE is not None
     if with_reference:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_TREE}"], check=True)
+        if REFERENCE_TREE is None:
+            raise FileNotFoundError("set DPG_REFERENCE_TREE to the reference source tree")
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", "refgpu", f"REF={REFERENCE_TREE}"], check=True)
 
 
 def _load(path: Path, sigs):
@@ -199,6 +222,8 @@ def pagerank_f64(in_off, in_col, outdeg, damping=0.85, total=1.0, init_zero=Fals
 
 def pagerank_ref_f32(in_off, in_col, outdeg, damping=0.5, total=1000.0, init_zero=True, max_iterations=10000,
                      epsilon=1e-13) -> tuple[np.ndarray, int]:
+    """The reference's FP32 PageRank loop (defaults: its own parameters). epsilon < 0: exactly
+    max_iterations sweeps."""
     in_off, in_col, outdeg = _i32(in_off), _i32(in_col), _i32(outdeg)
     V = in_off.shape[0] - 1
     r = np.empty(max(V, 1), np.float32)
@@ -214,6 +239,53 @@ def pagerank_omp_f32(in_off, in_col, outdeg, damping=0.85, total=1.0, iterations
     oracle_lib().oracle_pagerank_omp_f32(V, _p(in_off), _p(in_col), _p(outdeg), damping, total, iterations, _p(r),
                                          threads)
     return r[:V]
+
+
+def rmat_arcs(scale, E, seed, wmin=1, wmax=100, permute=True, weights=True, V=None, a=0.57, b=0.19, c=0.19):
+    """The benchmark's seeded R-MAT arc list (src, dst, w or None), generated on the CPU."""
+    V = (1 << scale) if V is None else V
+    src = np.empty(max(E, 1), np.int32)
+    dst = np.empty(max(E, 1), np.int32)
+    w = np.empty(max(E, 1), np.int32) if weights else None
+    rc = oracle_lib().oracle_rmat_arcs(scale, V, E, seed, a, b, c, wmin, wmax, 1 if permute else 0, _p(src), _p(dst),
+                                       _p(w) if weights else None)
+    if rc != 0:
+        raise RuntimeError(f"oracle_rmat_arcs failed ({rc})")
+    return src[:E], dst[:E], (w[:E] if weights else None)
+
+
+def csr_from_arcs(V, src, dst, w=None):
+    """convertCSR's arrays (off, col, w or None) from an arc list in input order."""
+    src, dst = _i32(src), _i32(dst)
+    E = src.shape[0]
+    off = np.empty(V + 1, np.int32)
+    col = np.empty(max(E, 1), np.int32)
+    wo = np.empty(max(E, 1), np.int32) if w is not None else None
+    wi = _i32(w) if w is not None else None
+    rc = oracle_lib().oracle_csr_from_arcs(V, E, _p(src), _p(dst), _p(wi) if wi is not None else None, _p(off), _p(col),
+                                           _p(wo) if wo is not None else None)
+    if rc != 0:
+        raise RuntimeError(f"oracle_csr_from_arcs failed ({rc})")
+    return off, col[:E], (wo[:E] if wo is not None else None)
+
+
+def rmat_csr(scale, edge_factor, seed, wmin=1, wmax=100, permute=True, weights=True):
+    """(off, col, w or None) of the benchmark's R-MAT graph as the reference loader would build it."""
+    V = 1 << scale
+    src, dst, w = rmat_arcs(scale, edge_factor * V, seed, wmin, wmax, permute, weights)
+    return csr_from_arcs(V, src, dst, w)
+
+
+def csr_transpose(off, col):
+    """invertGraph's arrays (in_off, in_col)."""
+    off, col = _i32(off), _i32(col)
+    V = off.shape[0] - 1
+    in_off = np.empty(V + 1, np.int32)
+    in_col = np.empty(max(col.shape[0], 1), np.int32)
+    rc = oracle_lib().oracle_csr_transpose(V, _p(off), _p(col), _p(in_off), _p(in_col))
+    if rc != 0:
+        raise RuntimeError(f"oracle_csr_transpose failed ({rc})")
+    return in_off, in_col[:col.shape[0]]
 
 
 def color(off, col) -> tuple[np.ndarray, int]:
