@@ -48,7 +48,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["dpg", "reference"], default="dpg")
     ap.add_argument("--no-extra", action="store_true", help="skip the SpMV / SSSP / BFS side measurements")
-    ap.add_argument("--workload", choices=["pagerank", "spmv", "sssp", "bfs", "adjoint", "prgrad", "batch", "cdp", "grid"],
+    ap.add_argument("--workload", choices=["pagerank", "pagerank-large", "spmv", "sssp", "bfs", "adjoint", "prgrad",
+                                           "batch", "cdp", "grid"],
                     default="pagerank",
                     help="pagerank is the headline; the others print their own line (used for profiling)")
     ap.add_argument("--scale", type=int, default=0, help="R-MAT scale for --workload spmv/sssp/bfs")
@@ -739,6 +740,10 @@ def run_single_workload(args, world=1, rank=0, local=0):
         g = dpg.rmat_csr(scale, 16, seed=scale, weights=False)
         res = measure_cdp(dpg, ctx, torch, g)
         res["gteps"] = g.E / (res["persistent"]["ms"] / 1e3) / 1e9
+    elif args.workload == "pagerank-large":
+        scale = args.scale or 24
+        g = dpg.rmat_csr(scale, 16, seed=scale, wmin=1, wmax=255)
+        res = measure_pagerank_large(dpg, ctx, torch, g, peak, steps=max(1, min(args.steps, 5)))
     elif args.workload == "prgrad":
         scale = args.scale or 20
         g = dpg.rmat_csr(scale, 16, seed=scale, weights=False)

@@ -129,3 +129,50 @@ def test_random_direction_central_difference_fp64(ctx):
     v64, x64 = vals_np.astype(np.float64), X_np.astype(np.float64)
     num = (loss(v64 + eps * dv, x64 + eps * dXd) - loss(v64 - eps * dv, x64 - eps * dXd)) / (2 * eps)
     assert abs(ana - num) <= 1e-4 * max(1.0, abs(num))
+
+
+def test_backward_full_size_rmat22_64rhs_vs_fp64_sample(ctx):
+    """The stated adjoint configuration at its size: R-MAT scale 22 (67,108,864 arcs), FP32 values
+    lognormal(0, 1), 64 right-hand sides. dX = A^T G and dA are checked in FP64 on a seeded 1 % of
+    the vertices (every arc into each sampled vertex) and 1 % of the arcs, each entry within
+    1e-5 x its sum of |terms|."""
+    import torch
+
+    g = dpg.rmat_csr(22, 16, seed=22, weights=False)
+    V, E, nrhs = g.V, g.E, 64
+    dev = torch.device("cuda", 0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(5)
+    vals = torch.exp(torch.randn(E, device=dev, generator=gen))
+    X = torch.rand((V, nrhs), device=dev, generator=gen) * 2 - 1
+    G = torch.rand((V, nrhs), device=dev, generator=gen) * 2 - 1
+    dX = torch.empty((V, nrhs), device=dev)
+    dA = torch.empty(E, device=dev)
+    dg = dpg.Graph(ctx, g.offsets, g.col)
+    dpg.spmv_bwd_dev(ctx, dg, vals.data_ptr(), nrhs, X.data_ptr(), G.data_ptr(), dX.data_ptr(), dA.data_ptr())
+    ctx.synchronize()
+    rng = np.random.default_rng(22)
+    v_np = vals.cpu().numpy().astype(np.float64)
+    # dX rows of a 1 % vertex sample, from the transposed CSR (arc permutation gives each in-arc's value).
+    t_off, t_col, t_arc = dpg.csr_transpose_perm(V, g.offsets, g.col)
+    js = np.sort(rng.choice(V, V // 100, replace=False))
+    lo, hi = t_off[js].astype(np.int64), t_off[js + 1].astype(np.int64)
+    cnt = hi - lo
+    idx = np.repeat(lo - np.cumsum(cnt) + cnt, cnt) + np.arange(cnt.sum())
+    seg = np.repeat(np.arange(js.size), cnt)
+    G_rows = G[torch.from_numpy(t_col[idx].astype(np.int64)).to(dev)].cpu().numpy().astype(np.float64)
+    terms = v_np[t_arc[idx]][:, None] * G_rows
+    exp = np.zeros((js.size, nrhs))
+    mag = np.zeros((js.size, nrhs))
+    np.add.at(exp, seg, terms)
+    np.add.at(mag, seg, np.abs(terms))
+    got = dX[torch.from_numpy(js.astype(np.int64)).to(dev)].cpu().numpy()
+    assert np.all(np.abs(got - exp) <= TOL * mag + 1e-30)
+    # dA on a 1 % arc sample.
+    es = np.sort(rng.choice(E, E // 100, replace=False))
+    rows = np.searchsorted(g.offsets, es, side="right") - 1
+    Gr = G[torch.from_numpy(rows.astype(np.int64)).to(dev)].cpu().numpy().astype(np.float64)
+    Xc = X[torch.from_numpy(g.col[es].astype(np.int64)).to(dev)].cpu().numpy().astype(np.float64)
+    prod = Gr * Xc
+    got_a = dA[torch.from_numpy(es.astype(np.int64)).to(dev)].cpu().numpy()
+    assert np.all(np.abs(got_a - prod.sum(axis=1)) <= TOL * np.abs(prod).sum(axis=1) + 1e-30)
