@@ -1399,7 +1399,12 @@ dpg_status dpg_spmm_f32_dev(dpg_ctx* c, const dpg_graph* gc, const float* d_vals
         arena(c, S_SPMM_PARTIAL, static_cast<size_t>(g->spmm_plan.nseg + 1) * nrhs * 4, &st));
     if (st != DPG_OK) return st;
     c->last_host_iterations = 1;
-    DPG_CUDA_TRY(launch_spmm(g->spmm_plan, g->col, d_vals, d_X, nrhs, d_Y, partial, c->stream, c->sm_count, &c->prof));
+    if (spmm_group_ok(nrhs, d_X, d_Y, partial, nullptr))
+        DPG_CUDA_TRY(launch_spmm_group(g->spmm_plan, g->col, d_vals, d_X, nrhs, d_Y, partial, c->stream, c->sm_count,
+                                       &c->prof));
+    else
+        DPG_CUDA_TRY(launch_spmm(g->spmm_plan, g->col, d_vals, d_X, nrhs, d_Y, partial, c->stream, c->sm_count,
+                                 &c->prof));
     return DPG_OK;
 }
 
@@ -1412,6 +1417,19 @@ dpg_status dpg_spmv_bwd_f32_dev(dpg_ctx* c, const dpg_graph* gc, const float* d_
     if (g->V == 0) return DPG_OK;
     if (!d_G || (d_dA && !d_X) || (g->E > 0 && !d_vals)) return set_error(DPG_ERR_INVALID_ARG, "null vals/X/G");
     c->last_host_iterations = 1;
+    if (spmm_group_ok(nrhs, d_X, d_G, d_dX, nullptr) && (d_dX || d_dA)) {
+        // Both outputs in one pass over the transposed CSR: each arc's row of G is gathered once.
+        DPG_TRY(ensure_spmm_transpose(g));
+        dpg_status st = DPG_OK;
+        float* partial = static_cast<float*>(
+            arena(c, S_SPMM_PARTIAL, static_cast<size_t>(g->spmm_t_plan.nseg + 1) * nrhs * 4, &st));
+        if (st != DPG_OK) return st;
+        if (!spmm_group_ok(nrhs, partial, nullptr, nullptr, nullptr))
+            return set_error(DPG_ERR_CUDA, "misaligned workspace");
+        DPG_CUDA_TRY(launch_spmv_bwd_group(g->spmm_t_plan, g->tt_col, g->tt_arc, d_vals, d_X, d_G, nrhs, d_dX, partial,
+                                           d_dA, c->stream, c->sm_count, &c->prof));
+        return DPG_OK;
+    }
     if (d_dX) {
         DPG_TRY(ensure_spmm_transpose(g));
         dpg_status st = DPG_OK;

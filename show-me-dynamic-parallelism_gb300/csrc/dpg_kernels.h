@@ -199,6 +199,16 @@ struct SpmmPlanDev {
     int32_t nseg = 0;
 };
 void build_spmm_plan(const int32_t* off, int32_t V, SpmmPlanHost* plan);
+// The group kernels (8 lanes per row piece, float4 loads) take nrhs a multiple of 32 (up to 128)
+// and 16-byte aligned row blocks; spmm_group_ok says whether the given pointers qualify.
+bool spmm_group_ok(int nrhs, const void* a, const void* b, const void* c, const void* d);
+cudaError_t launch_spmm_group(const SpmmPlanDev& P, const int32_t* col, const float* val, const float* X, int nrhs,
+                              float* Y, float* partial, cudaStream_t s, int sm_count, LaunchHook* hook);
+// One pass over the transposed CSR (plan TP, columns tcol, arc permutation tarc): dX = A^T G and
+// dA[e] = <G[row(e)], X[col(e)]>; either output may be null.
+cudaError_t launch_spmv_bwd_group(const SpmmPlanDev& TP, const int32_t* tcol, const int32_t* tarc, const float* val,
+                                  const float* X, const float* G, int nrhs, float* dX, float* partial, float* dA,
+                                  cudaStream_t s, int sm_count, LaunchHook* hook);
 // Y[row][:] = sum over the row's arcs of val[e] * X[col[e]][:] (row-major [*][nrhs], nrhs <= 128);
 // partial holds nseg rows of nrhs.
 cudaError_t launch_spmm(const SpmmPlanDev& P, const int32_t* col, const float* val, const float* X, int nrhs, float* Y,

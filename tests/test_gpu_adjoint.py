@@ -176,3 +176,52 @@ def test_backward_full_size_rmat22_64rhs_vs_fp64_sample(ctx):
     prod = Gr * Xc
     got_a = dA[torch.from_numpy(es.astype(np.int64)).to(dev)].cpu().numpy()
     assert np.all(np.abs(got_a - prod.sum(axis=1)) <= TOL * np.abs(prod).sum(axis=1) + 1e-30)
+
+
+def test_group_and_general_paths_agree(ctx, cases):
+    """nrhs = 64 with 16-byte aligned rows takes the group kernels (float4 rows, one pass for dX and
+    dA); the same data at a 4-byte offset takes the general kernels. Both within the FP64 bound, and
+    the Inf rows of a vertex that no arc touches stay out of every result."""
+    import torch
+
+    h = cases["hubby"]
+    # The hub graph plus one isolated vertex, whose rows of X and G hold Inf.
+    g = dpg.csr_from_arcs(h.V + 1, np.repeat(np.arange(h.V), np.diff(h.offsets)), h.col)
+    lonely = h.V
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(9)
+    nrhs = 64
+    vals = np.exp(rng.normal(0, 1, g.E)).astype(np.float32)
+    X = rng.uniform(-1, 1, (g.V, nrhs)).astype(np.float32)
+    G = rng.uniform(-1, 1, (g.V, nrhs)).astype(np.float32)
+    X[lonely] = np.inf
+    G[lonely] = np.inf
+    dg = dpg.Graph(ctx, g.offsets, g.col)
+    tv = torch.from_numpy(vals).to(dev)
+    outs = {}
+    for off in (0, 1):
+        bX = torch.zeros(g.V * nrhs + off, device=dev)
+        bG = torch.zeros(g.V * nrhs + off, device=dev)
+        bX[off:] = torch.from_numpy(X.ravel()).to(dev)
+        bG[off:] = torch.from_numpy(G.ravel()).to(dev)
+        dX = torch.empty(g.V * nrhs + off, device=dev)
+        dA = torch.empty(g.E, device=dev)
+        Y = torch.empty(g.V * nrhs + off, device=dev)
+        dpg.spmv_bwd_dev(ctx, dg, tv.data_ptr(), nrhs, bX[off:].data_ptr(), bG[off:].data_ptr(), dX[off:].data_ptr(),
+                         dA.data_ptr())
+        dpg.spmm_dev(ctx, dg, tv.data_ptr(), nrhs, bX[off:].data_ptr(), Y[off:].data_ptr())
+        ctx.synchronize()
+        outs[off] = (dX[off:].view(g.V, nrhs).cpu().numpy(), dA.cpu().numpy(), Y[off:].view(g.V, nrhs).cpu().numpy())
+    A = _matrix(g, vals)
+    Aabs = abs(A)
+    X64 = np.where(np.isinf(X), 0, X).astype(np.float64)
+    G64 = np.where(np.isinf(G), 0, G).astype(np.float64)
+    rows = np.repeat(np.arange(g.V), np.diff(g.offsets))
+    keep = np.ones(g.V, bool)
+    keep[lonely] = False
+    for off, (dX, dA, Y) in outs.items():
+        assert np.all(np.abs(dX - A.T @ G64)[keep] <= TOL * (Aabs.T @ np.abs(G64))[keep] + 1e-30), off
+        assert np.all(np.abs(Y - A @ X64)[keep] <= TOL * (Aabs @ np.abs(X64))[keep] + 1e-30), off
+        prod = G64[rows] * X64[g.col]
+        assert np.all(np.abs(dA - prod.sum(axis=1)) <= TOL * np.abs(prod).sum(axis=1) + 1e-30), off
+        assert np.all(np.isfinite(dA))
