@@ -490,6 +490,10 @@ def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=51
     t0 = time.perf_counter()
     tuning = b.autotune(src)
     t_tune = time.perf_counter() - t0
+    gt = b.graph_tuning()
+    settings: dict[str, int] = {}
+    for h, c in zip(gt["hub_threshold"].tolist(), gt["chunk"].tolist()):
+        settings[f"hub{h}_chunk{c}"] = settings.get(f"hub{h}_chunk{c}", 0) + 1
     pr = {"iterations": sweeps, "damping": DAMPING, "total_rank": 1.0}
     b.run(src, dist.data_ptr(), rank_v.data_ptr(), pr_opts_=pr)  # capture
     ctx.synchronize()
@@ -573,7 +577,7 @@ def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=51
             "sources_per_graph": nsrc, "pagerank_sweeps": sweeps, "vertices": V, "arcs": E,
             "ms_batch": t_batch, "ms_loop": t_loop, "speedup": t_loop / t_batch,
             "gteps_batch": arcs / (t_batch / 1e3) / 1e9, "gteps_loop": arcs / (t_loop / 1e3) / 1e9,
-            "tuning": tuning, "kernels_per_batch": b.launches(), "plain_calls": len(mine) * (nsrc + 1),
+            "tuning": tuning, "graphs_per_sssp_setting": settings, "kernels_per_batch": b.launches(), "plain_calls": len(mine) * (nsrc + 1),
             "sssp_bit_exact_vs_plain": sssp_equal, "pagerank_max_err_over_max_rank": pr_err,
             "s_generate": t_gen, "s_pack": t_pack, "s_autotune": t_tune, **split}
 

@@ -212,8 +212,16 @@ dpg_status dpg_batch_create(dpg_ctx* ctx, int32_t ngraphs, const int32_t* vstart
                             const int32_t* col, const int32_t* weights, dpg_batch** out);
 dpg_status dpg_batch_destroy(dpg_batch* b);
 dpg_status dpg_batch_info(const dpg_batch* b, int32_t* ngraphs, int32_t* V, int64_t* E);
+/* Batch-wide tuning; setting it also drops any per-graph SSSP setting. */
 dpg_status dpg_batch_set_tuning(dpg_batch* b, const dpg_batch_tuning* t);
 dpg_status dpg_batch_get_tuning(const dpg_batch* b, dpg_batch_tuning* t);
+/* Per-graph SSSP binning: hub_threshold[g] (>= 1) and chunk[g] (128 / 256 / 512) for each of the n
+ * graphs. The graphs that share a setting are solved by one multi-source launch; the launches of
+ * the settings run one after another in the same solve. Both NULL: every graph uses the batch-wide
+ * tuning again. Results never depend on these settings. dpg_batch_get_graph_tuning fills n entries
+ * each with the setting every graph runs with. */
+dpg_status dpg_batch_set_graph_tuning(dpg_batch* b, const int32_t* hub_threshold, const int32_t* chunk);
+dpg_status dpg_batch_get_graph_tuning(const dpg_batch* b, int32_t* hub_threshold, int32_t* chunk);
 /* SSSP from nsrc (1..32) sources of every graph in one persistent launch: h_sources[g * nsrc + k] is
  * a vertex of graph g (local id); d_dist[v * nsrc + k] = distance of union vertex v from source k of
  * v's graph (DPG_INF_COST when unreachable). Distances are exactly those of dpg_sssp on each graph
@@ -230,8 +238,13 @@ dpg_status dpg_batch_run(dpg_ctx* ctx, dpg_batch* b, int32_t nsrc, const int32_t
                          const dpg_expand_opts* sssp_opts, int32_t* d_dist, const dpg_pr_opts* pr_opts, float* d_rank);
 /* Kernel launches in one replay of the captured graph. */
 dpg_status dpg_batch_launches(const dpg_batch* b, int64_t* kernels_per_run);
-/* Times candidate tunings on this batch (SSSP binning on one source per graph; PageRank hot-cache
- * size on three sweeps), keeps the fastest in the batch and returns it. Results never depend on it. */
+/* Tunes the batch and keeps the result in it. SSSP binning per graph: the graphs fall into size
+ * classes by arc count (below 2^17, below 2^21, the rest); each class's 12 candidate settings
+ * (hub_threshold 16/32/64/128 x chunk 128/256/512) are timed on one source per graph of the class,
+ * and every graph takes its class's fastest (dpg_batch_get_graph_tuning). PageRank's shared-memory
+ * hot-cache size is timed on three sweeps of the whole batch (one gather serves every graph).
+ * `chosen` gets the batch-wide summary: the setting of the class holding the most arcs, and the
+ * hot-cache size. Results never depend on the tuning. */
 dpg_status dpg_batch_autotune(dpg_ctx* ctx, dpg_batch* b, int32_t nsrc, const int32_t* h_sources,
                               dpg_batch_tuning* chosen);
 

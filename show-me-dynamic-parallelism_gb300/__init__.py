@@ -178,6 +178,8 @@ _SIGS = {
     "dpg_batch_run": [_P, _P, c_int32, _P, _P, _P, _P, _P],
     "dpg_batch_launches": [_P, POINTER(c_int64)],
     "dpg_batch_autotune": [_P, _P, c_int32, _P, _P],
+    "dpg_batch_set_graph_tuning": [_P, _P, _P],
+    "dpg_batch_get_graph_tuning": [_P, _P, _P],
     "dpg_partition_lpt": [c_int32, _P, c_int32, _P, _P],
     "dpg_bfs_cdp_dev": [_P, _P, c_int32, c_int32, c_int32, _P, _P],
     "dpg_csr_transpose_dev": [_P, c_int32, c_int64, _P, _P, _P, _P, _P],
@@ -574,6 +576,23 @@ class Batch:
     def tuning(self, d: dict) -> None:
         t = BatchTuning(d["hub_threshold"], d["chunk"], d["pr_hot"])
         _check(lib().dpg_batch_set_tuning(self.handle, byref(t)))
+
+    def graph_tuning(self) -> dict:
+        """The SSSP setting each graph runs with: {"hub_threshold": [n], "chunk": [n]}."""
+        hub = np.empty(self.n, np.int32)
+        chunk = np.empty(self.n, np.int32)
+        _check(lib().dpg_batch_get_graph_tuning(self.handle, _ptr(hub), _ptr(chunk)))
+        return {"hub_threshold": hub, "chunk": chunk}
+
+    def set_graph_tuning(self, hub_threshold=None, chunk=None) -> None:
+        """Per-graph SSSP settings (both None: back to the batch-wide one)."""
+        if hub_threshold is None and chunk is None:
+            _check(lib().dpg_batch_set_graph_tuning(self.handle, None, None))
+            return
+        hub, ch = _i32(hub_threshold), _i32(chunk)
+        if hub.shape != (self.n,) or ch.shape != (self.n,):
+            raise ValueError("one hub_threshold and one chunk per graph")
+        _check(lib().dpg_batch_set_graph_tuning(self.handle, _ptr(hub), _ptr(ch)))
 
     def close(self) -> None:
         if self.handle:

@@ -13,8 +13,13 @@
 //              of each graph, (1-d) T / V_g + d D_g / V_g, comes from a per-graph dangling sum
 //              reduced over fixed pieces of the graph-major dangling list in a fixed order.
 //   CUDA graph both solves captured once (kernels and memsets only) and replayed per call.
-//   Autotuner  times the hub threshold and chunk size of the SSSP binning (one source per graph)
-//              and the shared-memory hot-cache size of the gather (a few sweeps), keeps the fastest.
+//   Autotuner  picks the hub threshold and chunk size of the SSSP binning per graph: graphs fall into
+//              size classes by arc count, each class's candidates are timed on one source per
+//              graph of the class, and every graph takes its class's fastest. Graphs of one setting
+//              form one multi-source launch; the launches of the groups run one after another
+//              (labels filled once, by the first), and their graphs' vertices are disjoint. The
+//              gather's shared-memory hot-cache size is timed for the batch as a whole: one sweep
+//              serves every graph, and the hot cache is a per-launch resource.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -119,6 +124,20 @@ struct dpg_batch {
     int32_t* d_src = nullptr;
     int64_t src_version = 0;
     dpg_batch_tuning tune{32, 256, -1};
+    // Per-graph SSSP binning (empty: every graph uses tune.hub_threshold and tune.chunk).
+    std::vector<int32_t> g_hub, g_chunk;
+    int64_t tuning_version = 0;
+    // Graphs grouped by SSSP setting, each group with its sources as label indices; rebuilt when the
+    // sources or the settings change.
+    struct Group {
+        int32_t hub;
+        int32_t chunk;
+        int32_t* d_src;
+        int32_t nsources;
+    };
+    std::vector<Group> groups;
+    int64_t groups_src_version = -1;
+    int64_t groups_tuning_version = -1;
     // Captured solve: recorded on a private stream (the context stream may be the legacy default
     // stream, which cannot be captured) and launched on the context stream.
     cudaStream_t cap_stream = nullptr;
@@ -129,7 +148,14 @@ struct dpg_batch {
 
 namespace {
 
+void free_groups(dpg_batch* b) {
+    for (auto& gr : b->groups) cudaFree(gr.d_src);
+    b->groups.clear();
+    b->groups_src_version = b->groups_tuning_version = -1;
+}
+
 void batch_free(dpg_batch* b) {
+    free_groups(b);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
@@ -257,26 +283,35 @@ dpg_status run_batch_pagerank(dpg_batch* b, const PrBuffers& pb, const dpg_pr_op
     return DPG_OK;
 }
 
-struct SsspPlan {
-    ExpandWorkspace ws;
-    MultiExpandLaunch L;
+struct GroupLaunch {
+    int32_t hub;
+    int32_t chunk;
+    const int32_t* d_src;  // label indices of the group's sources
+    int32_t nsources;
 };
 
-// Workspace of the multi-source expansion; allocates, so it runs before capture.
-dpg_status sssp_plan(dpg_batch* b, int32_t nsrc, const int32_t* d_src, int32_t nsources, const dpg_expand_opts* in,
+struct SsspPlan {
+    ExpandWorkspace ws;  // shared by the groups' launches, sized for the largest need
+    std::vector<MultiExpandLaunch> L;
+};
+
+// Workspace and launches of the multi-source expansion, one launch per group; allocates, so it runs
+// before capture. An explicit in->hub_threshold overrides every group's.
+dpg_status sssp_plan(dpg_batch* b, int32_t nsrc, const std::vector<GroupLaunch>& groups, const dpg_expand_opts* in,
                      int32_t* d_dist, SsspPlan* sp) {
     dpg_ctx* c = b->ctx;
     dpg_expand_opts o;
     fill_expand_defaults(in, &o, b->out);
-    const int32_t hub = (in && in->hub_threshold > 0) ? in->hub_threshold : b->tune.hub_threshold;
-    const int32_t chunk = b->tune.chunk;
     if (nsrc < 1 || nsrc > 32) return set_error(DPG_ERR_INVALID_ARG, "1 to 32 sources per graph");
     if (static_cast<int64_t>(b->V) * nsrc > INT32_MAX - 64)
         return set_error(DPG_ERR_CAPACITY, "sources x vertices must stay below 2^31");
+    auto hub_of = [&](const GroupLaunch& g) { return (in && in->hub_threshold > 0) ? in->hub_threshold : g.hub; };
     ExpandWorkspace& ws = sp->ws;
     memset(&ws, 0, sizeof(ws));
     ws.cap_v = static_cast<int64_t>(b->V) + 1;
-    ws.cap_chunks = expand_chunk_capacity(b->V, b->E, hub, chunk);
+    ws.cap_chunks = 1;
+    for (const GroupLaunch& g : groups)
+        ws.cap_chunks = std::max(ws.cap_chunks, expand_chunk_capacity(b->V, b->E, hub_of(g), g.chunk));
     ws.bmp_words = 1;
     dpg_status st = DPG_OK;
     const size_t nv = static_cast<size_t>(ws.cap_v);
@@ -294,32 +329,77 @@ dpg_status sssp_plan(dpg_batch* b, int32_t nsrc, const int32_t* d_src, int32_t n
     unsigned long long* d0 = static_cast<unsigned long long*>(arena(c, S_DIRTY0, static_cast<size_t>(b->V) * 8, &st));
     unsigned long long* d1 = static_cast<unsigned long long*>(arena(c, S_DIRTY1, static_cast<size_t>(b->V) * 8, &st));
     if (st != DPG_OK) return st;
-    MultiExpandLaunch& L = sp->L;
-    memset(&L, 0, sizeof(L));
-    L.off = b->out->off;
-    L.adj = b->out->adj;
-    L.V = b->V;
-    L.nsrc = nsrc;
-    L.dirty[0] = d0;
-    L.dirty[1] = d1;
-    L.label = d_dist;
-    L.sources = d_src;
-    L.nsources = nsources;
-    L.hub_threshold = hub;
-    L.chunk = chunk;
-    L.max_iter = o.max_iterations;
-    L.timeout_ns = static_cast<unsigned long long>(o.timeout_seconds * 1e9);
+    sp->L.clear();
+    for (size_t k = 0; k < groups.size(); ++k) {
+        MultiExpandLaunch L;
+        memset(&L, 0, sizeof(L));
+        L.off = b->out->off;
+        L.adj = b->out->adj;
+        L.V = b->V;
+        L.nsrc = nsrc;
+        L.dirty[0] = d0;
+        L.dirty[1] = d1;
+        L.label = d_dist;
+        L.sources = groups[k].d_src;
+        L.nsources = groups[k].nsources;
+        L.hub_threshold = hub_of(groups[k]);
+        L.chunk = groups[k].chunk;
+        L.max_iter = o.max_iterations;
+        L.timeout_ns = static_cast<unsigned long long>(o.timeout_seconds * 1e9);
+        L.skip_fill = k > 0 ? 1 : 0;  // the first launch fills every label and mark
+        sp->L.push_back(L);
+    }
     return DPG_OK;
 }
 
 dpg_status run_batch_sssp(dpg_batch* b, const SsspPlan& sp, LaunchHook* hook) {
     dpg_ctx* c = b->ctx;
     int grid = 0;
-    DPG_CUDA_TRY(launch_expand_multi(sp.L, sp.ws, c->st, c->stream, c->sm_count, &grid, hook));
+    for (const MultiExpandLaunch& L : sp.L)
+        DPG_CUDA_TRY(launch_expand_multi(L, sp.ws, c->st, c->stream, c->sm_count, &grid, hook));
     c->last_grid = grid;
     c->last_block = 256;
     c->last_host_iterations = -1;
     return DPG_OK;
+}
+
+int32_t graph_hub(const dpg_batch* b, int32_t g) { return b->g_hub.empty() ? b->tune.hub_threshold : b->g_hub[g]; }
+int32_t graph_chunk(const dpg_batch* b, int32_t g) { return b->g_chunk.empty() ? b->tune.chunk : b->g_chunk[g]; }
+
+// The groups of graphs that share an SSSP setting, with their sources (after set_sources).
+dpg_status ensure_groups(dpg_batch* b) {
+    if (b->groups_src_version == b->src_version && b->groups_tuning_version == b->tuning_version) return DPG_OK;
+    free_groups(b);
+    std::vector<std::pair<std::pair<int32_t, int32_t>, std::vector<int32_t>>> sets;
+    for (int32_t g = 0; g < b->n; ++g) {
+        const std::pair<int32_t, int32_t> key(graph_hub(b, g), graph_chunk(b, g));
+        auto it = std::find_if(sets.begin(), sets.end(), [&](const auto& x) { return x.first == key; });
+        if (it == sets.end()) {
+            sets.push_back({key, {}});
+            it = sets.end() - 1;
+        }
+        for (int32_t k = 0; k < b->nsrc; ++k) it->second.push_back(b->h_src[static_cast<size_t>(g) * b->nsrc + k]);
+    }
+    std::sort(sets.begin(), sets.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+    for (const auto& set : sets) {
+        dpg_batch::Group gr{set.first.first, set.first.second, nullptr, static_cast<int32_t>(set.second.size())};
+        dpg_status st = upload(b->ctx, &gr.d_src, set.second.data(), set.second.size());
+        if (st != DPG_OK) {
+            free_groups(b);
+            return st;
+        }
+        b->groups.push_back(gr);
+    }
+    DPG_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+    b->groups_src_version = b->src_version;
+    b->groups_tuning_version = b->tuning_version;
+    return DPG_OK;
+}
+
+std::vector<GroupLaunch> group_launches(const dpg_batch* b) {
+    std::vector<GroupLaunch> v;
+    for (const auto& gr : b->groups) v.push_back({gr.hub, gr.chunk, gr.d_src, gr.nsources});
+    return v;
 }
 
 // Sources of every graph as label indices (copy c = source number within its graph).
@@ -517,6 +597,9 @@ dpg_status dpg_batch_set_tuning(dpg_batch* b, const dpg_batch_tuning* t) {
     if (t->chunk != 128 && t->chunk != 256 && t->chunk != 512)
         return set_error(DPG_ERR_INVALID_ARG, "chunk must be 128, 256 or 512");
     b->tune = *t;
+    b->g_hub.clear();  // the batch-wide setting applies to every graph again
+    b->g_chunk.clear();
+    ++b->tuning_version;
     return DPG_OK;
 }
 
@@ -526,14 +609,45 @@ dpg_status dpg_batch_get_tuning(const dpg_batch* b, dpg_batch_tuning* t) {
     return DPG_OK;
 }
 
+dpg_status dpg_batch_set_graph_tuning(dpg_batch* b, const int32_t* hub_threshold, const int32_t* chunk) {
+    if (!b) return set_error(DPG_ERR_INVALID_ARG, "null batch");
+    if (!hub_threshold && !chunk) {
+        b->g_hub.clear();
+        b->g_chunk.clear();
+        ++b->tuning_version;
+        return DPG_OK;
+    }
+    if (!hub_threshold || !chunk) return set_error(DPG_ERR_INVALID_ARG, "give both per-graph arrays, or neither");
+    for (int32_t g = 0; g < b->n; ++g) {
+        if (hub_threshold[g] < 1)
+            return set_error(DPG_ERR_INVALID_ARG, "hub_threshold of graph " + std::to_string(g) + " must be >= 1");
+        if (chunk[g] != 128 && chunk[g] != 256 && chunk[g] != 512)
+            return set_error(DPG_ERR_INVALID_ARG, "chunk of graph " + std::to_string(g) + " must be 128, 256 or 512");
+    }
+    b->g_hub.assign(hub_threshold, hub_threshold + b->n);
+    b->g_chunk.assign(chunk, chunk + b->n);
+    ++b->tuning_version;
+    return DPG_OK;
+}
+
+dpg_status dpg_batch_get_graph_tuning(const dpg_batch* b, int32_t* hub_threshold, int32_t* chunk) {
+    if (!b || !hub_threshold || !chunk) return set_error(DPG_ERR_INVALID_ARG, "null batch or output");
+    for (int32_t g = 0; g < b->n; ++g) {
+        hub_threshold[g] = graph_hub(b, g);
+        chunk[g] = graph_chunk(b, g);
+    }
+    return DPG_OK;
+}
+
 dpg_status dpg_batch_sssp_dev(dpg_ctx* c, dpg_batch* b, int32_t nsrc, const int32_t* h_sources,
                               const dpg_expand_opts* opts, int32_t* d_dist) {
     DPG_TRY(use_device(c));
     DPG_TRY(check_batch(c, b));
     if (!d_dist) return set_error(DPG_ERR_INVALID_ARG, "null output");
     DPG_TRY(set_sources(b, nsrc, h_sources));
+    DPG_TRY(ensure_groups(b));
     SsspPlan sp;
-    DPG_TRY(sssp_plan(b, nsrc, b->d_src, b->n * nsrc, opts, d_dist, &sp));
+    DPG_TRY(sssp_plan(b, nsrc, group_launches(b), opts, d_dist, &sp));
     return run_batch_sssp(b, sp, &c->prof);
 }
 
@@ -560,8 +674,9 @@ dpg_status dpg_batch_run(dpg_ctx* c, dpg_batch* b, int32_t nsrc, const int32_t* 
     if (o.epsilon > 0) return set_error(DPG_ERR_UNSUPPORTED, "batched PageRank runs a fixed number of sweeps");
     DPG_TRY(set_sources(b, nsrc, h_sources));
     // Everything that allocates or synchronises happens here, outside the capture.
+    DPG_TRY(ensure_groups(b));
     SsspPlan sp;
-    DPG_TRY(sssp_plan(b, nsrc, b->d_src, b->n * nsrc, sssp_opts, d_dist, &sp));
+    DPG_TRY(sssp_plan(b, nsrc, group_launches(b), sssp_opts, d_dist, &sp));
     PrBuffers pb;
     DPG_TRY(pr_buffers(b, &pb));
     // The captured graph is reused while the launch arguments are unchanged.
@@ -570,7 +685,7 @@ dpg_status dpg_batch_run(dpg_ctx* c, dpg_batch* b, int32_t nsrc, const int32_t* 
         const unsigned char* q = static_cast<const unsigned char*>(p);
         key.insert(key.end(), q, q + n);
     };
-    put(&sp.L, sizeof(sp.L));
+    for (const MultiExpandLaunch& L : sp.L) put(&L, sizeof(L));
     put(&sp.ws, sizeof(sp.ws));
     put(&pb, sizeof(pb));
     put(&o, sizeof(o));
@@ -602,7 +717,7 @@ dpg_status dpg_batch_run(dpg_ctx* c, dpg_batch* b, int32_t nsrc, const int32_t* 
             return set_error(DPG_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(ei));
         }
         b->key.swap(key);
-        b->replay_launches = 3 + pr_launches(o.iterations);
+        b->replay_launches = 3 * static_cast<int64_t>(sp.L.size()) + pr_launches(o.iterations);
     }
     DPG_CUDA_TRY(cudaGraphLaunch(b->exec, c->stream));
     c->last_host_iterations = -1;
@@ -620,48 +735,71 @@ dpg_status dpg_batch_autotune(dpg_ctx* c, dpg_batch* b, int32_t nsrc, const int3
     DPG_TRY(use_device(c));
     DPG_TRY(check_batch(c, b));
     DPG_TRY(set_sources(b, nsrc, h_sources));
-    // SSSP binning: the first source of each graph per candidate, best of two timed runs.
+    // SSSP binning per graph. Graphs fall into size classes by arc count (below 2^17, below 2^21,
+    // the rest); each class's candidates are timed on the first source of each of its graphs alone
+    // (one launch, best of two after a warm-up), and every graph of the class takes the fastest.
     int32_t* dist = nullptr;
     DPG_CUDA_TRY(cudaMalloc(&dist, sizeof(int32_t) * (b->V > 0 ? b->V : 1)));
     const dpg_batch_tuning saved = b->tune;
     dpg_batch_tuning best = saved;
-    float best_ms = 1e30f;
+    std::vector<int32_t> hub(static_cast<size_t>(b->n), saved.hub_threshold), chunk(static_cast<size_t>(b->n), saved.chunk);
+    const std::vector<int32_t>& h_off = b->out->h_off;
+    auto arcs_of = [&](int32_t g) {
+        return static_cast<int64_t>(h_off[b->h_vstart[g + 1]]) - h_off[b->h_vstart[g]];
+    };
+    auto class_of = [&](int32_t g) { return arcs_of(g) < (1 << 17) ? 0 : arcs_of(g) < (1 << 21) ? 1 : 2; };
+    int64_t class_arcs[3] = {0, 0, 0};
     dpg_status st = DPG_OK;
-    for (int32_t hub : {16, 32, 64, 128}) {
-        for (int32_t chunk : {128, 256, 512}) {
-            b->tune.hub_threshold = hub;
-            b->tune.chunk = chunk;
-            SsspPlan sp;
-            // The first source of each graph alone (label index = its vertex when nsrc is 1).
-            std::vector<int32_t> first(static_cast<size_t>(b->n));
-            for (int32_t g = 0; g < b->n; ++g) first[g] = b->h_src[static_cast<size_t>(g) * nsrc] / nsrc;
-            int32_t* d_first = nullptr;
-            st = upload(c, &d_first, first.data(), first.size());
-            if (st == DPG_OK) st = sssp_plan(b, 1, d_first, b->n, nullptr, dist, &sp);
-            if (st == DPG_OK) {
-                run_batch_sssp(b, sp, nullptr);  // warm-up
-                st = check_device(c);
+    for (int cls = 0; cls < 3 && st == DPG_OK; ++cls) {
+        std::vector<int32_t> first;
+        for (int32_t g = 0; g < b->n; ++g)
+            if (class_of(g) == cls) {
+                first.push_back(b->h_src[static_cast<size_t>(g) * nsrc] / nsrc);  // label index of nsrc = 1
+                class_arcs[cls] += arcs_of(g);
             }
-            float t = 1e30f;
-            if (st == DPG_OK) t = time_ms(c, [&] { return run_batch_sssp(b, sp, nullptr); }, 2, &st);
-            cudaStreamSynchronize(c->stream);
-            cudaFree(d_first);
-            if (st != DPG_OK) break;
-            if (t < best_ms) {
-                best_ms = t;
-                best.hub_threshold = hub;
-                best.chunk = chunk;
+        if (first.empty()) continue;
+        int32_t* d_first = nullptr;
+        st = upload(c, &d_first, first.data(), first.size());
+        float best_ms = 1e30f;
+        int32_t best_hub = saved.hub_threshold, best_chunk = saved.chunk;
+        for (int32_t h : {16, 32, 64, 128}) {
+            for (int32_t ch : {128, 256, 512}) {
+                if (st != DPG_OK) break;
+                SsspPlan sp;
+                st = sssp_plan(b, 1, {{h, ch, d_first, static_cast<int32_t>(first.size())}}, nullptr, dist, &sp);
+                if (st == DPG_OK) {
+                    run_batch_sssp(b, sp, nullptr);  // warm-up
+                    st = check_device(c);
+                }
+                const float t = st == DPG_OK ? time_ms(c, [&] { return run_batch_sssp(b, sp, nullptr); }, 2, &st) : 1e30f;
+                if (st == DPG_OK && t < best_ms) {
+                    best_ms = t;
+                    best_hub = h;
+                    best_chunk = ch;
+                }
             }
         }
-        if (st != DPG_OK) break;
+        cudaStreamSynchronize(c->stream);
+        cudaFree(d_first);
+        for (int32_t g = 0; g < b->n; ++g)
+            if (class_of(g) == cls) {
+                hub[g] = best_hub;
+                chunk[g] = best_chunk;
+            }
     }
     cudaFree(dist);
     if (st != DPG_OK) {
         b->tune = saved;
         return st;
     }
-    b->tune.hub_threshold = best.hub_threshold;
-    b->tune.chunk = best.chunk;
+    // The batch-wide summary is the setting of the class holding the most arcs.
+    const int big = static_cast<int>(std::max_element(class_arcs, class_arcs + 3) - class_arcs);
+    for (int32_t g = 0; g < b->n; ++g)
+        if (class_of(g) == big) {
+            best.hub_threshold = hub[g];
+            best.chunk = chunk[g];
+            break;
+        }
     // Gather hot-cache size: three sweeps per candidate.
     PrBuffers pb;
     st = pr_buffers(b, &pb);
@@ -692,6 +830,9 @@ dpg_status dpg_batch_autotune(dpg_ctx* c, dpg_batch* b, int32_t nsrc, const int3
         return st;
     }
     b->tune = best;
+    b->g_hub.swap(hub);
+    b->g_chunk.swap(chunk);
+    ++b->tuning_version;
     if (chosen) *chosen = best;
     return DPG_OK;
 }

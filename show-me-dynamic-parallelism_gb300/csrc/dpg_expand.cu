@@ -973,12 +973,14 @@ __global__ void expand_init_kernel(ExpandParams P, int32_t source, int32_t init_
     }
 }
 
-// Multi-source start, part 1: every label to infinity, marks, bitmaps and counters cleared.
-__global__ void multi_fill_kernel(ExpandParams P, int64_t nlabels) {
+// Multi-source start, part 1: every label to infinity, marks, bitmaps and counters cleared. A
+// launch that continues a solve (another group of graphs, nlabels = nmarks = 0) clears only the
+// queue counters, so the arcs and pops statistics add up over the solve's launches.
+__global__ void multi_fill_kernel(ExpandParams P, int64_t nlabels, int64_t nmarks) {
     const int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t i = tid; i < nlabels; i += stride) P.label[i] = DPG_INF_COST;
-    for (int64_t v = tid; v < P.V; v += stride) {
+    for (int64_t v = tid; v < nmarks; v += stride) {
         P.dirty[0][v] = 0ull;
         P.dirty[1][v] = 0ull;
     }
@@ -988,9 +990,11 @@ __global__ void multi_fill_kernel(ExpandParams P, int64_t nlabels) {
             P.ws.ccount[k] = 0u;
         }
         P.st->bar_count = 0u;
-        P.st->iterations = 0ull;
-        P.st->edges = 0ull;
-        P.st->pops = 0ull;
+        if (nmarks > 0) {
+            P.st->iterations = 0ull;
+            P.st->edges = 0ull;
+            P.st->pops = 0ull;
+        }
     }
 }
 
@@ -1119,7 +1123,8 @@ cudaError_t run_multi(const MultiExpandLaunch& L, const ExpandWorkspace& ws, Dev
     const int64_t nlabels = static_cast<int64_t>(L.V) * L.nsrc;
     {
         HookScope hs(hook, DPG_KERNEL_INIT, stream);
-        multi_fill_kernel<<<sm_count * 8, kBlock, 0, stream>>>(P, nlabels);
+        multi_fill_kernel<<<sm_count * 8, kBlock, 0, stream>>>(P, L.skip_fill ? 0 : nlabels,
+                                                                L.skip_fill ? 0 : static_cast<int64_t>(L.V));
         if (L.nsources > 0)
             multi_seed_kernel<CH><<<(L.nsources + kBlock - 1) / kBlock, kBlock, 0, stream>>>(P, L.sources, L.nsources);
     }

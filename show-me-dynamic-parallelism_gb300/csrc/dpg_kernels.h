@@ -101,6 +101,9 @@ struct MultiExpandLaunch {
     int32_t chunk;
     int32_t max_iter;
     unsigned long long timeout_ns;
+    // Non-zero: the labels and marks were filled by an earlier launch of the same solve (another
+    // group of graphs with other settings, over disjoint vertices); only the counters are reset.
+    int32_t skip_fill;
 };
 cudaError_t launch_expand_multi(const MultiExpandLaunch& L, const ExpandWorkspace& ws, DevStatus* st,
                                 cudaStream_t stream, int sm_count, int* grid_out, LaunchHook* hook);

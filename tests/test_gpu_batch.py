@@ -158,6 +158,60 @@ def test_autotune_picks_a_candidate_and_changes_nothing(ctx, batch_case):
     b.tuning = saved
 
 
+def test_per_graph_tuning_changes_nothing(ctx, batch_case):
+    """Mixed per-graph SSSP settings run as one launch per setting; the distances (and the captured
+    graph's replays) equal those of one batch-wide setting, and the batch-wide setter drops them."""
+    import torch
+
+    gs, src, b = batch_case
+    d1, r1 = _device(NSRC * b.V, torch.int32), _device(b.V, torch.float32)
+    b.run(src, d1.data_ptr(), r1.data_ptr(), pr_opts_={"iterations": SWEEPS})
+    ctx.synchronize()
+    saved = b.tuning
+    rng = np.random.default_rng(11)
+    hub = rng.choice([1, 16, 64, 128, 100000], b.n).astype(np.int32)
+    chunk = rng.choice([128, 256, 512], b.n).astype(np.int32)
+    b.set_graph_tuning(hub, chunk)
+    t = b.graph_tuning()
+    assert np.array_equal(t["hub_threshold"], hub) and np.array_equal(t["chunk"], chunk)
+    groups = len(set(zip(hub.tolist(), chunk.tolist())))
+    assert groups > 1
+    d2, r2 = _device(NSRC * b.V, torch.int32), _device(b.V, torch.float32)
+    d2.fill_(-1)
+    b.sssp_dev(src, d2.data_ptr())
+    ctx.synchronize()
+    assert torch.equal(d1, d2)
+    for _ in range(2):  # capture, then replay
+        d2.fill_(-1)
+        b.run(src, d2.data_ptr(), r2.data_ptr(), pr_opts_={"iterations": SWEEPS})
+        ctx.synchronize()
+        assert torch.equal(d1, d2)
+        assert torch.equal(r1.view(torch.int32), r2.view(torch.int32))
+    assert b.launches() == 3 * groups + 3 + 3 * SWEEPS
+    bad = chunk.copy()
+    bad[2] = 100
+    with pytest.raises(dpg.DpgError):
+        b.set_graph_tuning(hub, bad)
+    b.tuning = saved  # the batch-wide setter applies to every graph again
+    t = b.graph_tuning()
+    assert np.all(t["hub_threshold"] == saved["hub_threshold"]) and np.all(t["chunk"] == saved["chunk"])
+
+
+def test_autotune_chooses_per_size_class(ctx, batch_case):
+    gs, src, b = batch_case
+    saved = b.tuning
+    b.autotune(src)
+    t = b.graph_tuning()
+    arcs = np.array([g.E for g in gs])
+    cls = np.where(arcs < (1 << 17), 0, np.where(arcs < (1 << 21), 1, 2))
+    for c in np.unique(cls):
+        sel = cls == c
+        assert len(set(t["hub_threshold"][sel].tolist())) == 1 and len(set(t["chunk"][sel].tolist())) == 1
+    assert set(t["hub_threshold"].tolist()) <= {16, 32, 64, 128}
+    assert set(t["chunk"].tolist()) <= {128, 256, 512}
+    b.tuning = saved
+
+
 def test_batch_rejects_bad_input(ctx, batch_case):
     import torch
 
