@@ -680,7 +680,59 @@ def measure_pagerank_large(dpg, ctx, torch, g, peak, steps=5):
     return out
 
 
-def extra_measurements(dpg, ctx, torch, g, peak, steps):
+def host_cpu() -> dict:
+    model = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")) or line.startswith("CPU part"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    import platform
+
+    return {"cores": os.cpu_count(), "machine": platform.machine(), "model": model}
+
+
+def cpu_baselines(dpg, g22, in_off, in_col, od, g24) -> dict:
+    """The CPU restatements, one thread and all threads, timed once each on the GPU host (the
+    reference's only CPU algorithm is bfs_cpu, restated as oracle.bfs; it has no CPU SSSP, SpMV or
+    PageRank). Bounded samples: one SpMV, one PageRank sweep, one BFS and one Dijkstra solve."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+
+    nall = orc.num_threads()  # read before any call sets a thread count (the setting persists)
+    out = {"host": host_cpu(), "threads_all": nall}
+
+    def timed(fn):
+        t0 = time.perf_counter()
+        fn()
+        return time.perf_counter() - t0
+
+    rng = np.random.default_rng(22)
+    vals = (1.0 - rng.random(g22.E, dtype=np.float32)).astype(np.float32)
+    x = rng.uniform(-1, 1, g22.V).astype(np.float32)
+    for th, tag in ((1, "1_thread"), (nall, "all_threads")):
+        t = timed(lambda: orc.spmv_omp_f32(g22.offsets, g22.col, vals, x, threads=th))
+        out[f"spmv_rmat22_{tag}"] = {"gteps": g22.E / t / 1e9, "s": t}
+        t = timed(lambda: orc.pagerank_omp_f32(in_off, in_col, od, iterations=1, threads=th))
+        out[f"pagerank_sweep_rmat22_{tag}"] = {"gteps": g22.E / t / 1e9, "s": t}
+    deg = np.diff(g24.offsets)
+    s24 = int(np.random.default_rng(24).choice(np.flatnonzero(deg > 0)))
+    t = timed(lambda: orc.bfs(g24.offsets, g24.col, s24))
+    out["bfs_rmat24_1_thread_bfs_cpu_restated"] = {"gteps": g24.E / t / 1e9, "s": t}
+    t = timed(lambda: orc.bfs_omp(g24.offsets, g24.col, s24, threads=nall))
+    out["bfs_rmat24_all_threads"] = {"gteps": g24.E / t / 1e9, "s": t}
+    gw = dpg.rmat_csr(22, 16, seed=22, wmin=1, wmax=255)
+    s22 = int(np.random.default_rng(22).choice(np.flatnonzero(np.diff(gw.offsets) > 0)))
+    t = timed(lambda: orc.sssp_dijkstra(gw.offsets, gw.col, gw.weights, s22))
+    out["sssp_rmat22_1_thread_dijkstra"] = {"gteps": gw.E / t / 1e9, "s": t}
+    t = timed(lambda: orc.sssp_bf_omp(gw.offsets, gw.col, gw.weights, s22, threads=nall))
+    out["sssp_rmat22_all_threads_frontier_bf"] = {"gteps": gw.E / t / 1e9, "s": t}
+    return out
+
+
+def extra_measurements(dpg, ctx, torch, g, peak, steps, pr_inputs=None):
     """SpMV and the SpMV adjoint on the scale-22 graph; SSSP, BFS and PageRank on R-MAT scale 24; the
     PageRank edge-weight gradient on scale 20; the 512-graph batch; the recursive CDP2 BFS variants against
     the persistent BFS on scale 16 (device-resident, CUDA events)."""
@@ -690,6 +742,8 @@ def extra_measurements(dpg, ctx, torch, g, peak, steps):
     out["sssp_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "sssp")
     out["bfs_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "bfs")
     out["pagerank_rmat24"] = measure_pagerank_large(dpg, ctx, torch, g24, peak)
+    if pr_inputs is not None:
+        out["cpu_baselines"] = cpu_baselines(dpg, g, *pr_inputs, g24)
     out.update(measure_grid(dpg, ctx, torch, peak))
     del g24
     g20 = dpg.rmat_csr(20, 16, seed=20, weights=False)
@@ -897,7 +951,7 @@ def run_dpg(args, world, rank, local):
             line["cpu_baseline"] = cpu_pagerank_sample(orc, in_off, in_col, od, E)
         if not args.no_extra:
             del gi
-            line["extra"] = extra_measurements(dpg, ctx, torch, g, peak, args.steps)
+            line["extra"] = extra_measurements(dpg, ctx, torch, g, peak, args.steps, (in_off, in_col, od))
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.barrier()
