@@ -110,7 +110,9 @@ struct BfsOp {
     static constexpr bool kPeek = true;
     static constexpr bool kMask = false;
     static constexpr int min_blocks(int) { return 3; }
-    __device__ __forceinline__ static int row_value(const ExpandParams& P, int u, int) { return __ldcg(P.label + u); }
+    // Levels are claimed once, level-synchronously (top-down pushes and bottom-up claims of
+    // iteration j both set j + 1), so a vertex popped in iteration j has level j: no load needed.
+    __device__ __forceinline__ static int row_value(const ExpandParams&, int, int j) { return j; }
     __device__ __forceinline__ static void load_edge(const ExpandParams& P, int e, int du, int& v, int& r,
                                                      int& cand) {
         v = __ldg(P.col + e);
@@ -205,6 +207,9 @@ struct PushCtx {
     unsigned* far_count;
     int* far_min;
     int threshold;
+    // Small iterations (latency-bound): each candidate head's row range is loaded with its label
+    // peek, so a push needs no further round trip.
+    bool early_rows;
     // The warp's push buffer in shared memory (see flush_pushes) and its share of the frontier
     // statistics, added to mf / nf once per iteration.
     int* buf_v;
@@ -469,6 +474,29 @@ __device__ __forceinline__ void relax_batch(const ExpandParams& P, const PushCtx
         for (int u = 0; u < U; ++u) Op::load_edge(P, act[u] ? e[u] : 0, du[u], v[u], row[u], cand[u]);
 #pragma unroll
         for (int u = 0; u < U; ++u) cur[u] = Op::kPeek ? __ldcg(P.label + v[u]) : 0;
+        if constexpr (U <= 4) {
+            if (Q.early_rows) {
+                // Row ranges of every candidate head, issued with the peeks (extra loads for heads
+                // that are not pushed; worth it only while an iteration is latency-bound).
+                int2 se[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) se[u] = make_int2(__ldg(P.off + row[u]), __ldg(P.off + row[u] + 1));
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    ok[u] = act[u] && Op::want(v[u], cand[u], cur[u]) && Op::commit(P, v[u], cand[u]);
+                if (Q.far) {
+                    bool far[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        far[u] = ok[u] && cand[u] >= Q.threshold;
+                        ok[u] = ok[u] && !far[u];
+                    }
+                    far_push<U>(P, Q, far, v, cand);
+                }
+                push_batch<Op, kClassify, CH, U>(P, Q, ok, v, row, se);
+                return;
+            }
+        }
 #pragma unroll
         for (int u = 0; u < U; ++u)
             ok[u] = act[u] && Op::want(v[u], cand[u], cur[u]) && Op::commit(P, v[u], cand[u]);
@@ -694,7 +722,7 @@ __global__ void __launch_bounds__(kBlock, Op::min_blocks(CH)) expand_kernel(Expa
                            kNearFar ? P.far[split ? (pile + 1) % 3 : pile] : nullptr,
                            kNearFar ? P.far_count + (split ? (pile + 1) % 3 : pile) : nullptr,
                            kNearFar ? P.far_min + (split ? (pile + 1) % 3 : pile) : nullptr, threshold,
-                           buffered ? p_v[warp] : nullptr, buffered ? p_se[warp] : nullptr,
+                           !buffered, buffered ? p_v[warp] : nullptr, buffered ? p_se[warp] : nullptr,
                            buffered ? &p_n[warp] : nullptr, &p_mf[warp], &p_nf[warp]};
         const int32_t* qv_cur = p ? P.ws.qv[1] : P.ws.qv[0];
         const int2* qse_cur = p ? P.ws.qse[1] : P.ws.qse[0];
