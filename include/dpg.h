@@ -132,6 +132,11 @@ dpg_status dpg_graph_info(const dpg_graph* g, int32_t* V, int64_t* E, int32_t* w
  * No counterpart in the reference. */
 dpg_status dpg_graph_plan_info(dpg_graph* g, int32_t* tiles, int32_t* hubs_small, int32_t* hubs_big,
                                int32_t* segments);
+/* Shared-memory hot cache of the row gathers (no counterpart in the reference): the number of
+ * renamed columns each CTA keeps in shared memory, and how many of the graph's arcs gather from
+ * them (builds the column renaming when needed; synchronises). The other arcs' gathers are the
+ * random reads that dpg_calibrate_random_reads bounds. */
+dpg_status dpg_graph_hot_cache(dpg_graph* g, int32_t* hot_entries, int64_t* hot_arcs);
 
 /* ---- SSSP (replaces SSSP_GPU, apps/sssp/src/sssp_wrapper.cu:304-341) --------------------------- */
 /* dist[v] = shortest distance from source, DPG_INF_COST when unreachable. Weights must be >= 0. */
@@ -324,6 +329,13 @@ dpg_status dpg_ctx_profile_read(dpg_ctx* ctx, int32_t kind, int64_t* launches, d
  * 4 int64 each (synchronises) and reports how many slots exist. */
 dpg_status dpg_ctx_trace_enable(dpg_ctx* ctx, int32_t max_iterations);
 dpg_status dpg_ctx_trace_read(dpg_ctx* ctx, int64_t* out, int32_t capacity, int32_t* count);
+
+/* ---- random-read ceiling (no counterpart in the reference) -------------------------------------- */
+/* Measures how many random 4-byte reads per second the device sustains from an array of n_floats
+ * floats (two 1024-thread CTAs per SM, 8 independent loads in flight per thread, `iters` rounds):
+ * the ceiling of the row gathers' and the expansion's scattered reads, beside HBM bandwidth. An
+ * array of 16 MB stays in L2; one of several GB is read from HBM. Allocates the array, synchronises. */
+dpg_status dpg_calibrate_random_reads(dpg_ctx* ctx, int64_t n_floats, int32_t iters, double* loads_per_second);
 
 /* ---- failure-detection self test --------------------------------------------------------------- */
 /* Runs the persistent kernel's grid barrier with one block missing, so its bounded wait must run

@@ -178,6 +178,8 @@ _SIGS = {
     "dpg_batch_run": [_P, _P, c_int32, _P, _P, _P, _P, _P],
     "dpg_batch_launches": [_P, POINTER(c_int64)],
     "dpg_batch_autotune": [_P, _P, c_int32, _P, _P],
+    "dpg_calibrate_random_reads": [_P, c_int64, c_int32, POINTER(c_double)],
+    "dpg_graph_hot_cache": [_P, POINTER(c_int32), POINTER(c_int64)],
     "dpg_batch_set_graph_tuning": [_P, _P, _P],
     "dpg_batch_get_graph_tuning": [_P, _P, _P],
     "dpg_partition_lpt": [c_int32, _P, c_int32, _P, _P],
@@ -482,6 +484,12 @@ class Graph:
         _check(lib().dpg_graph_plan_info(self.handle, byref(t), byref(hs), byref(hb), byref(sg)))
         return {"tiles": t.value, "hubs_small": hs.value, "hubs_big": hb.value, "segments": sg.value}
 
+    def hot_cache(self) -> dict:
+        """Shared-memory hot cache of the row gathers: entries kept per CTA and arcs served by them."""
+        n, a = c_int32(), c_int64()
+        _check(lib().dpg_graph_hot_cache(self.handle, byref(n), byref(a)))
+        return {"hot_entries": n.value, "hot_arcs": a.value}
+
     def set_relabel(self, enable: bool) -> None:
         """Column renaming by frequency for SpMV/PageRank (on by default; results are identical)."""
         _check(lib().dpg_graph_relabel(self.handle, 1 if enable else 0))
@@ -604,6 +612,13 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def calibrate_random_reads(ctx: Context, n_floats: int, iters: int = 400) -> float:
+    """Random 4-byte reads per second from an array of n_floats floats (see include/dpg.h)."""
+    r = c_double(0.0)
+    _check(lib().dpg_calibrate_random_reads(ctx.handle, n_floats, iters, byref(r)))
+    return float(r.value)
 
 
 CDP_NAIVE, CDP_WARP, CDP_BLOCK, CDP_GRID = 1, 2, 3, 4

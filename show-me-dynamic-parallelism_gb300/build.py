@@ -30,7 +30,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", 
 NVCC_FLAGS += os.environ.get("DPG_NVCC_EXTRA", "").split()
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wextra", "-Wno-unused-parameter"]
 
-LIB_CU = ["dpg_api.cu", "dpg_expand.cu", "dpg_rowgather.cu", "dpg_noalloc.cu", "dpg_layout.cu", "dpg_adjoint.cu", "dpg_prgrad.cu", "dpg_batch.cu", "dpg_cdp.cu", "dpg_transpose.cu"]
+LIB_CU = ["dpg_api.cu", "dpg_expand.cu", "dpg_rowgather.cu", "dpg_noalloc.cu", "dpg_layout.cu", "dpg_adjoint.cu", "dpg_prgrad.cu", "dpg_batch.cu", "dpg_cdp.cu", "dpg_transpose.cu", "dpg_calib.cu"]
 # Translation units with device-side launches (relocatable device code, linked with cudadevrt).
 RDC_CU = {"dpg_cdp.cu"}
 LIB_CXX = ["dpg_host.cpp"]

@@ -1336,6 +1336,44 @@ dpg_status dpg_graph_plan_info(dpg_graph* g, int32_t* tiles, int32_t* hubs_small
     return DPG_OK;
 }
 
+namespace {
+__global__ void count_below_kernel(const int32_t* __restrict__ col, int64_t E, int32_t bound,
+                                   unsigned long long* count) {
+    unsigned long long c = 0;
+    for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < E;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        c += __ldg(col + e) < bound ? 1ull : 0ull;
+    c = warp_sum_u64(c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+}  // namespace
+
+dpg_status dpg_graph_hot_cache(dpg_graph* g, int32_t* hot_entries_out, int64_t* hot_arcs) {
+    if (!g || !g->ctx) return set_error(DPG_ERR_INVALID_ARG, "null graph or destroyed context");
+    dpg_ctx* c = g->ctx;
+    DPG_TRY(use_device(c));
+    const int32_t hot = hot_entries(c, g);
+    if (hot_entries_out) *hot_entries_out = hot;
+    if (!hot_arcs) return DPG_OK;
+    *hot_arcs = 0;
+    if (hot == 0 || g->E == 0) return DPG_OK;
+    DPG_TRY(ensure_relabel(g));
+    unsigned long long* d = nullptr;
+    DPG_CUDA_TRY(cudaMalloc(&d, sizeof(unsigned long long)));
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long), c->stream);
+    if (e == cudaSuccess) {
+        count_below_kernel<<<c->sm_count * 4, 256, 0, c->stream>>>(g->pcol, g->E, hot, d);
+        e = cudaGetLastError();
+    }
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return set_error(DPG_ERR_CUDA, std::string("hot-cache count: ") + cudaGetErrorString(e));
+    *hot_arcs = static_cast<int64_t>(h);
+    return DPG_OK;
+}
+
 dpg_status dpg_sssp_dev(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_expand_opts* opts, int32_t* d_dist) {
     DPG_TRY(use_device(c));
     return run_expand(c, g, source, opts, d_dist, false);
