@@ -445,9 +445,21 @@ def measure_prgrad(dpg, ctx, torch, g, peak, reps=3):
     t_fwd, (nf, _) = timed(zero)   # zero seed: the adjoint loop stops after one sweep
     t_all, (nf2, na) = timed(seed)
     sweeps = nf2 + na + 2
+    # The loop the batched seed replaces: one gradient call per seed vertex (the loss is a sum over
+    # the subset, so the gradients add up). Timed on 4 of the seed vertices, scaled to all of them.
+    seeds = np.flatnonzero(seed_np)
+    one = torch.zeros(V, device=dev)
+    t_one = []
+    for v in seeds[:4]:
+        one.zero_()
+        one[int(v)] = 1.0
+        t_one.append(timed(one)[0])
+    loop_ms = statistics.mean(t_one) * len(seeds)
     return {"ms_total": t_all, "ms_forward_only": t_fwd, "forward_sweeps": nf2, "adjoint_sweeps": na,
             "ms_per_sweep": t_all / sweeps, "gteps_sweeps": sweeps * E / (t_all / 1e3) / 1e9,
-            "grad_over_forward": t_all / t_fwd, "rank_sum": float(r.double().sum())}
+            "grad_over_forward": t_all / t_fwd, "rank_sum": float(r.double().sum()),
+            "seed_vertices": int(len(seeds)), "ms_one_seed_vertex": statistics.mean(t_one),
+            "ms_loop_over_seed_vertices": loop_ms, "speedup_vs_loop": loop_ms / t_all}
 
 
 def measure_batch(dpg, ctx, torch, peak, ngraphs=512, nsrc=8, sweeps=20, seed=512, reps=3, rank=0, world=1):
