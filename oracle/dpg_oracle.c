@@ -186,10 +186,12 @@ int oracle_sssp_bf_omp(int32_t V, const int32_t* off, const int32_t* col, const 
 #pragma omp parallel for schedule(dynamic, 64)
         for (int64_t i = 0; i < n; ++i) {
             int32_t u = q0[i];
-            inq[u] = 0;
-            int32_t du;
-#pragma omp atomic read
-            du = dist[u];
+            /* Clear u's queued flag, then read its distance. Both sequentially consistent, as are
+             * the compare-and-swap and the exchange of a relaxer: otherwise the clear can wait in a
+             * store buffer while the read goes first, a concurrent improvement of u sees the flag
+             * still set and does not queue u, and that improvement is never relaxed. */
+            __atomic_store_n(&inq[u], (unsigned char)0, __ATOMIC_SEQ_CST);
+            int32_t du = __atomic_load_n(&dist[u], __ATOMIC_SEQ_CST);
             for (int32_t e = off[u]; e < off[u + 1]; ++e) {
                 int32_t v = col[e];
                 int32_t nd = du + w[e];
@@ -197,8 +199,8 @@ int oracle_sssp_bf_omp(int32_t V, const int32_t* off, const int32_t* col, const 
 #pragma omp atomic read
                 cur = dist[v];
                 while (nd < cur) {
-                    if (__atomic_compare_exchange_n(&dist[v], &cur, nd, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
-                        if (!__atomic_exchange_n(&inq[v], (unsigned char)1, __ATOMIC_RELAXED)) {
+                    if (__atomic_compare_exchange_n(&dist[v], &cur, nd, 0, __ATOMIC_SEQ_CST, __ATOMIC_RELAXED)) {
+                        if (!__atomic_exchange_n(&inq[v], (unsigned char)1, __ATOMIC_SEQ_CST)) {
                             int64_t pos = __atomic_fetch_add(&n1, 1, __ATOMIC_RELAXED);
                             q1[pos] = v;
                         }
