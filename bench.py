@@ -348,6 +348,39 @@ def measure_expand(dpg, ctx, torch, g, peak, kind, nsrc=8, seed=24, solution=Non
             "sources": srcs}
 
 
+def measure_mapping(dpg, ctx, torch, g, nsrc=2, seed=22):
+    """SSSP under each work mapping: the reference's solutions 0-4 (thread per vertex; rows of degree
+    >= 64 per warp, consolidated per warp, per CTA or grid-wide) and the binned default (warp
+    scan-gather, grid-wide chunks from degree 128). Median ms over nsrc sources; distances must agree
+    across every mapping."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    dg = dpg.Graph(ctx, g.offsets, g.col, g.weights)
+    deg = np.diff(g.offsets)
+    srcs = [int(s) for s in np.random.default_rng(seed).choice(np.flatnonzero(deg > 0), nsrc, replace=False)]
+    label = torch.empty(g.V, dtype=torch.int32, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    runs = [(dpg.SOLUTION_NAMES[s], {"solution": s}) for s in (dpg.SOL_THREAD, dpg.SOL_NAIVE, dpg.SOL_WARP,
+                                                              dpg.SOL_BLOCK, dpg.SOL_GRID, dpg.SOL_BINNED)]
+    out, ref = {}, [None] * nsrc
+    for name, opts in runs:
+        times, same = [], True
+        for k, s in enumerate(srcs):
+            dpg.sssp_dev(ctx, dg, s, label.data_ptr(), **opts)  # warm-up
+            ctx.synchronize()
+            e0.record()
+            dpg.sssp_dev(ctx, dg, s, label.data_ptr(), **opts)
+            e1.record()
+            torch.cuda.synchronize()
+            ctx.synchronize()
+            times.append(e0.elapsed_time(e1))
+            if ref[k] is None:
+                ref[k] = label.clone()
+            same = same and bool(torch.equal(ref[k], label))
+        out[name] = {"ms": statistics.median(times), "distances_equal": same}
+    dg.close()
+    return {"sources": srcs, "mappings": out}
+
+
 def measure_adjoint(dpg, ctx, torch, g, peak, nrhs=64, reps=5):
     """SpMV backward on g with lognormal(0,1) FP32 values and nrhs right-hand sides: the batched call
     (dX = A^T G and dA together) against looping the plain single-vector kernels once per column."""
@@ -755,6 +788,7 @@ def extra_measurements(dpg, ctx, torch, g, peak, steps, pr_inputs=None):
         "note": "random 4-byte reads, 2 x 1024-thread CTAs per SM, 8 loads in flight per thread"}}
     out["spmv_rmat22"] = measure_spmv(dpg, ctx, torch, g, peak, steps)
     out["spmv_bwd_rmat22_64rhs"] = measure_adjoint(dpg, ctx, torch, g, peak)
+    out["sssp_mapping_rmat22"] = measure_mapping(dpg, ctx, torch, dpg.rmat_csr(22, 16, seed=22, wmin=1, wmax=255))
     g24 = dpg.rmat_csr(24, 16, seed=24, wmin=1, wmax=255)
     out["sssp_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "sssp")
     out["bfs_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "bfs")

@@ -65,3 +65,32 @@ def test_no_reference_or_oracle_in_product_library():
     assert "oracle_" not in out and "ref_load" not in out
     deps = subprocess.run(["ldd", str(dpg.LIB_PATH)], capture_output=True, text=True).stdout
     assert "liboracle" not in deps and "libref" not in deps
+
+
+STRUCTS = {"dpg_expand_opts": "ExpandOpts", "dpg_pr_opts": "PrOpts", "dpg_run_stats": "RunStats",
+           "dpg_batch_tuning": "BatchTuning", "dpg_cdp_stats": "CdpStats", "dpg_host_graph": "_HostGraph"}
+
+
+def test_binding_structs_match_the_header(tmp_path):
+    """Size and every field offset of the option and result structs, from a C program compiled
+    against include/dpg.h, equal those of the Python binding's ctypes structures."""
+    import ctypes
+
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "dpg.h"', "int main(void) {"]
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(dpg, pyname)
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'    printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{ROOT / 'include'}", str(src), "-o", str(exe)], check=True)
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    want = []
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(dpg, pyname)
+        want.append(f"{cname} size {ctypes.sizeof(cls)}")
+        want += [f"{cname} {fname} {getattr(cls, fname).offset}" for fname, _ in cls._fields_]
+    assert got[:-1] == want
