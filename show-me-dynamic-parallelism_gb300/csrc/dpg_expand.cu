@@ -69,6 +69,9 @@ struct ExpandParams {
     int* far_min;         // [3] smallest distance pushed into each pile
     int64_t far_cap;
     int32_t delta;
+    // Multi-source SSSP: non-zero when nsrc is a multiple of 4 and the labels are 16-byte aligned,
+    // so a vertex's labels can be read four at a time (relax_mask_vec4).
+    int32_t label_vec4;
 };
 
 // Operator interface of the expansion:
@@ -184,6 +187,48 @@ __device__ __forceinline__ bool tag_or(unsigned long long* w, unsigned tag, unsi
         if (prev == old) return !fresh;
         old = prev;
     }
+}
+
+// Multi-source relaxation of one arc (tail labels lu, head labels lv, weight w) for the sources in
+// mask m, eight sources at a time: two 16-byte loads of the tail's labels and two of the head's,
+// then an atomicMin for every source whose candidate beats the head's label, all issued before any
+// result is used. Source by source, each needed a load and then its atomic, and an atomic keeps
+// the next source's loads from being issued ahead of it: two round trips per source in the mask
+// instead of two per eight. Returns the mask of the sources whose label of the head this call
+// lowered. Needs nsrc % 4 == 0 and 16-byte aligned labels; a group's upper four labels are read
+// only when the mask has a bit there, so nsrc = 4 (mod 8) reads nothing past the vertex.
+__device__ __forceinline__ unsigned relax_mask_vec4(int nsrc, const int32_t* lu, int32_t* lv, int w, unsigned m) {
+    unsigned bits = 0;
+    for (int g0 = 0; g0 < nsrc; g0 += 8) {
+        const unsigned mm = (m >> g0) & 0xFFu;
+        if (mm == 0u) continue;
+        const int4* tl = reinterpret_cast<const int4*>(lu + g0);
+        const int4* hl = reinterpret_cast<const int4*>(lv + g0);
+        int4 t0 = make_int4(0, 0, 0, 0), t1 = t0, h0 = t0, h1 = t0;
+        if (mm & 0x0Fu) {
+            t0 = __ldcg(tl);
+            h0 = __ldcg(hl);
+        }
+        if (mm & 0xF0u) {
+            t1 = __ldcg(tl + 1);
+            h1 = __ldcg(hl + 1);
+        }
+        const int t[8] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w};
+        const int h[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+        int cand[8], old[8];
+        unsigned want = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            cand[q] = t[q] + w;
+            if (((mm >> q) & 1u) && cand[q] < h[q]) want |= 1u << q;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) old[q] = ((want >> q) & 1u) ? atomicMin(lv + g0 + q, cand[q]) : 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (((want >> q) & 1u) && cand[q] < old[q]) bits |= 1u << (g0 + q);
+    }
+    return bits;
 }
 
 __device__ __forceinline__ int shfl_rv(int v, int src) { return __shfl_sync(kFullMask, v, src); }
@@ -458,11 +503,15 @@ __device__ __forceinline__ void relax_batch(const ExpandParams& P, const PushCtx
             const int32_t* lu = P.label + static_cast<int64_t>(du[u].x) * P.nsrc;
             int32_t* lv = P.label + static_cast<int64_t>(v[u]) * P.nsrc;
             unsigned bits = 0;
-            while (m) {
-                const int k = __ffs(m) - 1;
-                m &= m - 1u;
-                const int cand = __ldcg(lu + k) + w[u];
-                if (cand < __ldcg(lv + k) && cand < atomicMin(lv + k, cand)) bits |= 1u << k;
+            if (P.label_vec4) {
+                if (m) bits = relax_mask_vec4(P.nsrc, lu, lv, w[u], m);
+            } else {
+                while (m) {
+                    const int k = __ffs(m) - 1;
+                    m &= m - 1u;
+                    const int cand = __ldcg(lu + k) + w[u];
+                    if (cand < __ldcg(lv + k) && cand < atomicMin(lv + k, cand)) bits |= 1u << k;
+                }
             }
             ok[u] = bits != 0u && tag_or(Q.dirty + v[u], Q.tag, bits);
         }
@@ -1148,6 +1197,7 @@ cudaError_t run_multi(const MultiExpandLaunch& L, const ExpandWorkspace& ws, Dev
     P.nsrc = L.nsrc;
     P.dirty[0] = L.dirty[0];
     P.dirty[1] = L.dirty[1];
+    P.label_vec4 = (L.nsrc % 4 == 0 && (reinterpret_cast<uintptr_t>(L.label) & 15u) == 0) ? 1 : 0;
     const int64_t nlabels = static_cast<int64_t>(L.V) * L.nsrc;
     {
         HookScope hs(hook, DPG_KERNEL_INIT, stream);

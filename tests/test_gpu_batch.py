@@ -68,7 +68,7 @@ def test_batch_sssp_equals_plain_per_graph(ctx, batch_case):
         assert np.array_equal(d[v0:v1, 0], exact), k
 
 
-@pytest.mark.parametrize("nsrc", [1, 3, 32])
+@pytest.mark.parametrize("nsrc", [1, 3, 4, 12, 32])
 def test_batch_sssp_other_source_counts(ctx, batch_case, nsrc):
     import torch
 
@@ -88,6 +88,22 @@ def test_batch_sssp_other_source_counts(ctx, batch_case, nsrc):
         for c in range(nsrc):
             exact = oracle.sssp_dijkstra(g.offsets, g.col, g.weights, int(src[k, c]))
             assert np.array_equal(d[v0:v1, c], exact), (k, c)
+
+
+def test_batch_sssp_unaligned_labels(ctx, batch_case):
+    """Labels that do not start on a 16-byte boundary take the source-by-source relaxation; the
+    distances equal the aligned run's (which reads eight labels at a time)."""
+    import torch
+
+    gs, src, b = batch_case
+    aligned = _device(NSRC * b.V, torch.int32)
+    b.sssp_dev(src, aligned.data_ptr())
+    buf = _device(NSRC * b.V + 1, torch.int32)
+    buf.fill_(-5)
+    b.sssp_dev(src, buf.data_ptr() + 4)
+    ctx.synchronize()
+    assert int(buf[0]) == -5
+    assert torch.equal(buf[1:], aligned)
 
 
 def test_batch_pagerank_equals_plain_and_fp64(ctx, batch_case):
