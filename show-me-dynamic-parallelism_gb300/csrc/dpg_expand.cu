@@ -231,6 +231,80 @@ __device__ __forceinline__ unsigned relax_mask_vec4(int nsrc, const int32_t* lu,
     return bits;
 }
 
+// tag_or starting from a value of the word read earlier (`seen`): the first compare-and-swap goes out
+// at once, and a stale `seen` only costs a retry. Each failed swap means the word changed after
+// `seen` was read, at most nsrc + 1 times in an iteration, so the loop ends.
+__device__ __forceinline__ bool tag_or_from(unsigned long long* w, unsigned tag, unsigned bits,
+                                            unsigned long long seen) {
+    const unsigned long long tg = static_cast<unsigned long long>(tag) << 32;
+    unsigned long long old = seen;
+    for (;;) {
+        const bool fresh = (old >> 32) == static_cast<unsigned long long>(tag);
+        const unsigned long long want = fresh ? (old | bits) : (tg | bits);
+        if (want == old) return false;
+        const unsigned long long prev = atomicCAS(w, old, want);
+        if (prev == old) return !fresh;
+        old = prev;
+    }
+}
+
+// Up to 8 sources (nsrc <= 8, labels 16-byte aligned), G arcs at a time in three phases: the
+// tail's and head's labels of every arc (16-byte loads), then the atomicMin of every improving
+// source of every arc together with a read of each improved head's mark word, then the marks'
+// compare-and-swaps. A chain of three round trips per G arcs.
+template <int G>
+__device__ __forceinline__ void relax_mask8_group(const ExpandParams& P, unsigned long long* dirty, unsigned tag,
+                                                  const unsigned (&m)[G], const int (&tail)[G],
+                                                  const int (&head)[G], const int (&w)[G], bool (&ok)[G]) {
+    int4 t0[G], t1[G], h0[G], h1[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        const int4* tl = reinterpret_cast<const int4*>(P.label + static_cast<int64_t>(tail[g]) * P.nsrc);
+        const int4* hl = reinterpret_cast<const int4*>(P.label + static_cast<int64_t>(head[g]) * P.nsrc);
+        t0[g] = make_int4(0, 0, 0, 0);
+        t1[g] = t0[g];
+        h0[g] = t0[g];
+        h1[g] = t0[g];
+        if (m[g] & 0x0Fu) {
+            t0[g] = __ldcg(tl);
+            h0[g] = __ldcg(hl);
+        }
+        if (m[g] & 0xF0u) {
+            t1[g] = __ldcg(tl + 1);
+            h1[g] = __ldcg(hl + 1);
+        }
+    }
+    unsigned want[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        const int t[8] = {t0[g].x, t0[g].y, t0[g].z, t0[g].w, t1[g].x, t1[g].y, t1[g].z, t1[g].w};
+        const int h[8] = {h0[g].x, h0[g].y, h0[g].z, h0[g].w, h1[g].x, h1[g].y, h1[g].z, h1[g].w};
+        want[g] = 0u;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (((m[g] >> q) & 1u) && t[q] + w[g] < h[q]) want[g] |= 1u << q;
+    }
+    int old[G][8];
+    unsigned long long seen[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        const int t[8] = {t0[g].x, t0[g].y, t0[g].z, t0[g].w, t1[g].x, t1[g].y, t1[g].z, t1[g].w};
+        int32_t* lv = P.label + static_cast<int64_t>(head[g]) * P.nsrc;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) old[g][q] = ((want[g] >> q) & 1u) ? atomicMin(lv + q, t[q] + w[g]) : 0;
+        seen[g] = want[g] ? __ldcg(dirty + head[g]) : 0ull;
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        const int t[8] = {t0[g].x, t0[g].y, t0[g].z, t0[g].w, t1[g].x, t1[g].y, t1[g].z, t1[g].w};
+        unsigned bits = 0u;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (((want[g] >> q) & 1u) && t[q] + w[g] < old[g][q]) bits |= 1u << q;
+        ok[g] = bits != 0u && tag_or_from(dirty + head[g], tag, bits, seen[g]);
+    }
+}
+
 __device__ __forceinline__ int shfl_rv(int v, int src) { return __shfl_sync(kFullMask, v, src); }
 __device__ __forceinline__ int2 shfl_rv(int2 v, int src) {
     return make_int2(__shfl_sync(kFullMask, v.x, src), __shfl_sync(kFullMask, v.y, src));
@@ -497,6 +571,25 @@ __device__ __forceinline__ void relax_batch(const ExpandParams& P, const PushCtx
             }
             row[u] = v[u];
         }
+        if (P.label_vec4 && P.nsrc <= 8) {
+            constexpr int G = (U >= 2 && Op::min_blocks(CH) <= 2) ? 2 : 1;
+#pragma unroll
+            for (int u0 = 0; u0 < U; u0 += G) {
+                unsigned m[G];
+                int tail[G], head[G], wg[G];
+                bool okg[G];
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    m[g] = act[u0 + g] ? static_cast<unsigned>(du[u0 + g].y) : 0u;
+                    tail[g] = du[u0 + g].x;
+                    head[g] = v[u0 + g];
+                    wg[g] = w[u0 + g];
+                }
+                relax_mask8_group<G>(P, Q.dirty, Q.tag, m, tail, head, wg, okg);
+#pragma unroll
+                for (int g = 0; g < G; ++g) ok[u0 + g] = okg[g];
+            }
+        } else {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             unsigned m = act[u] ? static_cast<unsigned>(du[u].y) : 0u;
@@ -514,6 +607,7 @@ __device__ __forceinline__ void relax_batch(const ExpandParams& P, const PushCtx
                 }
             }
             ok[u] = bits != 0u && tag_or(Q.dirty + v[u], Q.tag, bits);
+        }
         }
     } else {
         // Inactive lanes load arc 0 (the adjacency always holds at least one entry) and the label of
