@@ -392,15 +392,13 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
 #pragma unroll
     for (int u = 0; u < U; ++u) any |= ok[u];
     if (!__any_sync(kFullMask, any)) return;
-    if (Op::kDedup) {
-        unsigned old[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) old[u] = ok[u] ? atomicOr(Q.bmp + (v[u] >> 5), 1u << (v[u] & 31)) : 0u;
-#pragma unroll
-        for (int u = 0; u < U; ++u) ok[u] = ok[u] && (old[u] & (1u << (v[u] & 31))) == 0u;
-    }
-    // Row ranges: loaded here, or passed in by a caller that fetched them ahead (se_pre[u]).
+    // Row ranges: passed in by a caller that fetched them ahead (se_pre[u]), or loaded here, issued
+    // together with the de-duplication atomics so the two share one round trip (a head that the
+    // bitmap then drops wasted its two loads).
     int s[U], e[U];
+    unsigned old[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) old[u] = (Op::kDedup && ok[u]) ? atomicOr(Q.bmp + (v[u] >> 5), 1u << (v[u] & 31)) : 0u;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         s[u] = 0;
@@ -412,6 +410,10 @@ __device__ __forceinline__ void push_batch(const ExpandParams& P, const PushCtx&
             s[u] = __ldg(P.off + row[u]);
             e[u] = __ldg(P.off + row[u] + 1);
         }
+    }
+    if (Op::kDedup) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) ok[u] = ok[u] && (old[u] & (1u << (v[u] & 31))) == 0u;
     }
     const int lane = lane_id();
     const unsigned lt = (1u << lane) - 1u;
