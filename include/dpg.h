@@ -301,9 +301,8 @@ dpg_status dpg_pagerank_f32_host(dpg_ctx* ctx, int32_t V, int64_t E, const int32
  * The graph is checked on the device before anything is relaxed: a violation of the ranges above
  * returns DPG_ERR_INVALID_ARG. Every call shares the array and clears what must start at zero;
  * calls whose GPU work overlaps (two threads or streams) race on it. The first call on a device
- * looks up the array's address (cudaGetSymbolAddress) and keeps it: make that first call before
- * any stream capture, and reload the library after a cudaDeviceReset of that device. Calls no
- * cudaMalloc, cudaFree or other allocating routine. */
+ * looks up the array's address (cudaGetSymbolAddress) and keeps it; reload the library after a
+ * cudaDeviceReset of that device. Calls no cudaMalloc, cudaFree or other allocating routine. */
 dpg_status dpg_sssp_noalloc_dev(int32_t V, int64_t E, const int32_t* d_offsets, const int32_t* d_adj_pairs,
                                 int32_t source, int32_t* d_dist, void* stream);
 

@@ -22,10 +22,9 @@
 //     E, neighbour ids in [0, V), weights in [0, 2^30)); a bad graph returns DPG_ERR_INVALID_ARG
 //     and nothing is relaxed;
 //   * the first call on a device looks up the array's device address (cudaGetSymbolAddress, which
-//     may load the module) and keeps it for later calls on that device; make that first call
-//     before any stream capture. The kept address belongs to the device's primary context as it
-//     was at that call: after cudaDeviceReset the library must be reloaded before this entry
-//     point is used again on that device.
+//     may load the module) and keeps it for later calls on that device. The kept address belongs
+//     to the device's primary context as it was at that call: after cudaDeviceReset the library
+//     must be reloaded before this entry point is used again on that device.
 
 #include <cuda_runtime.h>
 
