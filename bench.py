@@ -791,6 +791,14 @@ def extra_measurements(dpg, ctx, torch, g, peak, steps, pr_inputs=None):
     out["sssp_mapping_rmat22"] = measure_mapping(dpg, ctx, torch, dpg.rmat_csr(22, 16, seed=22, wmin=1, wmax=255))
     g24 = dpg.rmat_csr(24, 16, seed=24, wmin=1, wmax=255)
     out["sssp_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "sssp")
+    # SSSP against the random-read ceiling of its label array (16 M int32, 64 MB): every scanned
+    # arc peeks its head's label at a random address.
+    ceiling = dpg.calibrate_random_reads(ctx, g24.V)
+    r = out["sssp_rmat24"]
+    relax = r["edges_scanned_over_E"] * g24.E / (r["kernel_ms"] / 1e3)
+    r["random_read"] = {"label_array_mb": 4 * g24.V / 2**20, "ceiling_gloads_per_s": ceiling / 1e9,
+                        "scanned_arcs_per_s_g": relax / 1e9, "frac": relax / ceiling,
+                        "ceiling_source": "dpg_calibrate_random_reads on an array the size of the labels, this run"}
     out["bfs_rmat24"] = measure_expand(dpg, ctx, torch, g24, peak, "bfs")
     out["pagerank_rmat24"] = measure_pagerank_large(dpg, ctx, torch, g24, peak)
     if pr_inputs is not None:
