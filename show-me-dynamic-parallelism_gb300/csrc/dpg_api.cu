@@ -592,6 +592,7 @@ dpg_status run_expand(dpg_ctx* c, const dpg_graph* g, int32_t source, const dpg_
     L.source = source;
     L.bfs = bfs;
     L.solution = o.solution;
+    L.wide = g->max_degree >= o.hub_threshold || g->E > 8 * static_cast<int64_t>(g->V);
     L.threshold = o.threshold;
     L.hub_threshold = o.hub_threshold;
     L.max_iter = o.max_iterations;

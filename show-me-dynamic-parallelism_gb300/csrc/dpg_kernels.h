@@ -76,6 +76,9 @@ struct ExpandLaunch {
     int* far_min = nullptr;
     int64_t far_cap = 0;
     int32_t delta = 0;
+    // A graph with hubs or more than 8 arcs per vertex: the binned and direction-optimizing kernels
+    // run their build for more CTAs per SM (kWideBlocks in dpg_expand.cu).
+    bool wide = false;
 };
 
 // Chunk capacity per parity for a graph of V vertices and E arcs when vertices of degree >=
