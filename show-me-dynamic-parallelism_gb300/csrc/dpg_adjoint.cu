@@ -263,9 +263,12 @@ __global__ void __launch_bounds__(kBlock) spmm_group_kernel(const int4* __restri
 // float4 parts, then a 3-step butterfly) and written by the group's first lane. dX or dA may be
 // skipped (null). Measured on R-MAT 22 with 64 right-hand sides: 5.6 ms against 7.55 ms for the
 // two general kernels (row gather over the transpose, then an arc pass gathering X as well), and
-// 9.3 ms for two group kernels doing the same two passes.
+// 9.3 ms for two group kernels doing the same two passes. CTAs per SM: with 64 right-hand sides
+// (QPL = 2) the kernel takes 80 registers unbounded (3 CTAs); bounded to 4 CTAs (64 registers,
+// 128 bytes of spills) the call went from 5.57 to 5.30 ms on the same box. The other widths keep
+// what they take unbounded (47, 106 and 128 registers).
 template <int QPL>
-__global__ void __launch_bounds__(kBlock) spmv_bwd_group_kernel(const int4* __restrict__ items, int nitems,
+__global__ void __launch_bounds__(kBlock, QPL == 1 ? 5 : QPL == 2 ? 4 : 2) spmv_bwd_group_kernel(const int4* __restrict__ items, int nitems,
                                                                 const int32_t* __restrict__ tcol,
                                                                 const int32_t* __restrict__ tarc,
                                                                 const float* __restrict__ val,
