@@ -86,7 +86,7 @@ TRAFFIC_KERNEL = "rowgather_kernel"
 # The command whose ncu output --ingest-traffic turns into profiles/<TRAFFIC_FILE> (one launch,
 # one pass: DRAM bytes only, on the headline workload after 40 gather launches of warm-up).
 TRAFFIC_COMMAND = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none "
-                   "-k regex:rowgather_kernel -s 40 -c 1 --csv --page raw --log-file gpurun_out/traffic.csv "
+                   "-k regex:rowgather_kernel -s 40 -c 1 --csv --page raw --log-file traffic.csv "
                    "python bench.py --steps 3 --warmup 3 --no-extra --no-e2e")
 
 
@@ -120,7 +120,7 @@ def ingest_traffic(csv_path: str) -> int:
     out.write_text(
         f"# DRAM bytes of one {TRAFFIC_KERNEL} launch (PageRank sweep, R-MAT scale 22), from ncu.\n"
         f"# command: {TRAFFIC_COMMAND}\n"
-        f"# ingested by: python bench.py --ingest-traffic gpurun_out/traffic.csv\n"
+        f"# ingested by: python bench.py --ingest-traffic traffic.csv\n"
         f"sources_fingerprint = {sources_fingerprint()}\n"
         f"kernel = {r[names.index('Kernel Name')]}\n"
         f"dram__bytes_read.sum = {val['dram__bytes_read.sum'] * scale:.0f}\n"
