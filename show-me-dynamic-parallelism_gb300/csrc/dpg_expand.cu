@@ -812,19 +812,51 @@ __global__ void __launch_bounds__(kBlock, MINB > 0 ? MINB : Op::min_blocks(CH)) 
     int threshold = kNearFar ? P.delta : 0;
     int pile = 0;
     int j = 0;
+    // The iteration's counters. In the 3-CTA builds (sparse graphs, whose thousands of small
+    // iterations each pay this) one thread per CTA reads them and shares them: with every warp of
+    // 456 CTAs reading the same few words, the L2 served some 15 K requests to one line per
+    // iteration. Same box, alternated: 4096^2 grid BFS 51.9 -> 46.6 ms, near-far SSSP 66.1 ->
+    // 62.0 ms. The 4-CTA build (R-MAT graphs) reads them per warp: with the shared read its
+    // bottom-up BFS steps ran 10-50 % longer, though the frontiers and direction choices were
+    // the same.
+    constexpr bool kCtaCounters = (MINB == 0);
+    __shared__ unsigned s_ctr[3];
+    __shared__ int s_far_min;
+    __shared__ unsigned long long s_mf;
     for (;; ++j) {
         const int p = j & 1;
         // Counters can pass the capacities only after a push has already raised DPG_ERR_CAPACITY
         // (which stops the loop at the barrier); the clamps keep every read inside its buffer anyway.
-        const unsigned n = min(ld_volatile(P.ws.qcount + (j % 3)), static_cast<unsigned>(P.ws.cap_v));
-        const unsigned nch = min(ld_volatile(P.ws.ccount + (j % 3)), static_cast<unsigned>(P.ws.cap_chunks));
+        // The previous iteration's grid barrier (which starts and ends with __syncthreads) keeps
+        // the shared copies' writes after every thread's reads of the last values.
+        auto read_q = [&] { return min(ld_volatile(P.ws.qcount + (j % 3)), static_cast<unsigned>(P.ws.cap_v)); };
+        auto read_c = [&] { return min(ld_volatile(P.ws.ccount + (j % 3)), static_cast<unsigned>(P.ws.cap_chunks)); };
+        auto read_far_n = [&] {
+            return static_cast<unsigned>(min(static_cast<int64_t>(ld_volatile(P.far_count + pile)), P.far_cap));
+        };
+        auto read_far_min = [&] { return *reinterpret_cast<const volatile int*>(P.far_min + pile); };
+        auto read_mf = [&] { return *reinterpret_cast<const volatile unsigned long long*>(P.mf + j % 3); };
+        if constexpr (kCtaCounters) {
+            if (threadIdx.x == 0) {
+                s_ctr[0] = read_q();
+                s_ctr[1] = read_c();
+                if (kNearFar) {
+                    s_ctr[2] = read_far_n();
+                    s_far_min = read_far_min();
+                }
+                if (kDirOpt) s_mf = read_mf();
+            }
+            __syncthreads();
+        }
+        const unsigned n = kCtaCounters ? s_ctr[0] : read_q();
+        const unsigned nch = kCtaCounters ? s_ctr[1] : read_c();
         bool split = false;
         unsigned far_n = 0;
         if (kNearFar && n == 0 && nch == 0) {
-            far_n = static_cast<unsigned>(min(static_cast<int64_t>(ld_volatile(P.far_count + pile)), P.far_cap));
+            far_n = kCtaCounters ? s_ctr[2] : read_far_n();
             if (far_n == 0) break;
             split = true;
-            const int fmin = *reinterpret_cast<const volatile int*>(P.far_min + pile);
+            const int fmin = kCtaCounters ? s_far_min : read_far_min();
             const long long t = max(static_cast<long long>(threshold) + P.delta, static_cast<long long>(fmin) + 1);
             threshold = static_cast<int>(min(t, static_cast<long long>(0x7FFFFFFF)));
         }
@@ -834,9 +866,7 @@ __global__ void __launch_bounds__(kBlock, MINB > 0 ? MINB : Op::min_blocks(CH)) 
             break;
         }
         if (kDirOpt) {
-            const unsigned long long mf = *reinterpret_cast<const volatile unsigned long long*>(P.mf + j % 3);
-            const unsigned nf = ld_volatile(P.nf + j % 3);
-            (void)nf;
+            const unsigned long long mf = kCtaCounters ? s_mf : read_mf();
             bottom_up = static_cast<long long>(mf) * 4 > unexplored && static_cast<long long>(mf) > P.V;
             unexplored -= static_cast<long long>(mf);
         }
