@@ -83,8 +83,9 @@ struct ExpandParams {
 //   min_blocks(CH)         CTAs per SM the kernel is compiled for (its register budget). A bound is
 //                          always given: without one the compiler picks its own, and an explicit 1
 //                          lets it spend up to 110 registers where it would otherwise use 64.
-//                          Single-source SSSP on R-MAT scale 24 takes 8.6-9.1 ms at 3 CTAs (80
-//                          registers) against 9.3 ms at 2; at 4 the registers spill.
+//                          Single-source SSSP on R-MAT scale 24 took 8.6-9.1 ms at 3 CTAs (80
+//                          registers) against 9.3 ms at 2. The binned and direction-optimizing
+//                          kernels also have a kWideBlocks build for graphs with hubs.
 struct SsspOp {
     using RV = int;
     static constexpr bool kDedup = true;
