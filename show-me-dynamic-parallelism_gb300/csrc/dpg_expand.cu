@@ -938,7 +938,9 @@ __global__ void __launch_bounds__(kBlock, MINB > 0 ? MINB : Op::min_blocks(CH)) 
             // range), so the common cases (a parent at the first in-arc, no in-arcs) cost one chain of
             // round trips for all of them; the others go on arc by arc.
             // The parent test and the arcs counted are those of a one-vertex-at-a-time scan.
-            constexpr int kBu = 4;
+            // R-MAT 24, 8 sources, same box: 9.12 ms in all at 4 vertices per lane, 7.64 at 2, 8.17
+            // at 1 (4 ran the vertices that scan many in-arcs one after another in the lane).
+            constexpr int kBu = 2;
             const int64_t stride = static_cast<int64_t>(nwarps) * 32 * kBu;
             for (int64_t base = static_cast<int64_t>(gwarp) * 32 * kBu; base < P.V; base += stride) {
                 int vv[kBu], b[kBu], e[kBu], t0[kBu];

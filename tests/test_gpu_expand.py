@@ -124,6 +124,18 @@ def test_stats_report_work(ctx, graphs, devgraphs):
     assert st.iterations >= 2 and st.edges_scanned >= 0.5 * g.E and st.grid_blocks >= 152
 
 
+def test_wide_graphs_run_the_4_cta_build(ctx, graphs, devgraphs):
+    """Graphs with hubs (R-MAT) run the binned SSSP and direction-optimizing BFS with 4 CTAs per
+    SM; a hubless graph of at most 8 arcs per vertex (the 64 x 64 grid) with 3. Distances and
+    levels are exact either way (the other tests of this file)."""
+    sms = ctx.sm_count
+    for name, per_sm in (("rmat14", 4), ("grid64", 3)):
+        g, s = graphs[name]
+        for solve in (dpg.sssp, dpg.bfs):
+            solve(ctx, devgraphs[name], s, solution=dpg.SOL_BINNED if solve is dpg.sssp else dpg.SOL_DIROPT)
+            assert ctx.last_stats().grid_blocks == per_sm * sms, (name, solve.__name__)
+
+
 def test_single_vertex_and_isolated_source(ctx):
     g = dpg.Graph(ctx, np.array([0, 0], np.int32), np.zeros(0, np.int32), np.zeros(0, np.int32))
     assert dpg.sssp(ctx, g, 0).tolist() == [0]
