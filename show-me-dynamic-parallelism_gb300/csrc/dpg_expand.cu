@@ -967,11 +967,29 @@ __global__ void __launch_bounds__(kBlock, MINB > 0 ? MINB : Op::min_blocks(CH)) 
                     if (!unv[r]) continue;
                     int k = b[r];
                     if (!found[r]) {
-                        for (k = b[r] + 1; k < e[r]; ++k)
-                            if (__ldcg(P.label + __ldg(P.t_col + k)) == j) {
+                        // The rest of the in-arcs kBuArcs at a time: their tails, then the tails'
+                        // levels, loaded together; the first parent among them ends the scan, so
+                        // the count is that of an arc-by-arc scan (a few loads past it are spare).
+                        // R-MAT 24, 8 sources, same box: 7.63 ms in all arc by arc, 6.42 two at a
+                        // time, 6.08 four at a time; a uniform random graph (16 M vertices, 8 arcs
+                        // each) 2.05 -> 1.25 ms; the grid unchanged.
+                        constexpr int kBuArcs = 4;
+                        for (k = b[r] + 1; k < e[r]; k += kBuArcs) {
+                            int c[kBuArcs], l[kBuArcs];
+#pragma unroll
+                            for (int q = 0; q < kBuArcs; ++q) c[q] = k + q < e[r] ? __ldg(P.t_col + k + q) : -1;
+#pragma unroll
+                            for (int q = 0; q < kBuArcs; ++q) l[q] = c[q] >= 0 ? __ldcg(P.label + c[q]) : -1;
+                            int hit = -1;
+#pragma unroll
+                            for (int q = kBuArcs - 1; q >= 0; --q)
+                                if (l[q] == j) hit = q;
+                            if (hit >= 0) {
+                                k += hit;
                                 found[r] = true;
                                 break;
                             }
+                        }
                     }
                     my_edges += static_cast<unsigned long long>((found[r] ? k + 1 : e[r]) - b[r]);
                     if (found[r]) {
