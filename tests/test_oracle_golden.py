@@ -71,6 +71,20 @@ def test_dijkstra_equals_reference_schedule_fixed_point(orc, seed):
     assert np.array_equal(d1, d2) and np.array_equal(d1, d3)
 
 
+def test_bf_omp_repeated_runs_stay_exact(orc):
+    """The OpenMP Bellman-Ford (the timed CPU baseline) run many times: its queued flag is cleared
+    and its distance read with sequentially consistent accesses, so an improvement made while a
+    vertex is being popped is never lost (with a relaxed clear, about 1 run in 200 of this fixture
+    came out wrong)."""
+    graphs = []
+    for seed in range(4):
+        g = _random_graph(np.random.default_rng(seed), 300, 1500)
+        graphs.append((g, orc.sssp_dijkstra(g.offsets, g.col, g.weights, 0)))
+    for rep in range(150):
+        g, want = graphs[rep % 4]
+        assert np.array_equal(orc.sssp_bf_omp(g.offsets, g.col, g.weights, 0), want), rep
+
+
 def test_dijkstra_inf_semantics(orc):
     # A chain whose total reaches 2^30: the int relaxation never lowers an INF label with it.
     big = (1 << 30) - 10
