@@ -3,6 +3,8 @@ output (recorded in tests/golden by make_golden.py), and, where the reference tr
 reference's host code run live."""
 from __future__ import annotations
 
+import os
+
 import numpy as np
 import pytest
 
@@ -80,9 +82,10 @@ def test_bf_omp_repeated_runs_stay_exact(orc):
     for seed in range(4):
         g = _random_graph(np.random.default_rng(seed), 300, 1500)
         graphs.append((g, orc.sssp_dijkstra(g.offsets, g.col, g.weights, 0)))
+    threads = max(4, os.cpu_count() or 4)  # explicit: an earlier call may have left OpenMP at 1 thread
     for rep in range(150):
         g, want = graphs[rep % 4]
-        assert np.array_equal(orc.sssp_bf_omp(g.offsets, g.col, g.weights, 0), want), rep
+        assert np.array_equal(orc.sssp_bf_omp(g.offsets, g.col, g.weights, 0, threads=threads), want), rep
 
 
 def test_dijkstra_inf_semantics(orc):
